@@ -1,0 +1,269 @@
+"""ctypes binding of ``libcuscan_gb300.so`` (the C ABI declared in ``include/cuscan_gb300.h``).
+
+Status codes map to Python exceptions exactly as the reference maps ``HdbscanError``
+(crates/cuscan-python/src/hdbscan.rs:956-968): invalid config/input -> ValueError, backend
+unavailable/numerical -> RuntimeError, overflow/capacity -> OverflowError, memory -> MemoryError.
+There is no fallback: if the library or a CUDA device is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+OK, INVALID_CONFIG, INVALID_INPUT, BACKEND_UNAVAILABLE, NUMERICAL, OVERFLOW, CAPACITY, MEMORY = range(8)
+PRECISION_PLAIN = 0
+PRECISION_BF16_REFINED = 1
+
+_F32P = C.POINTER(C.c_float)
+_F64P = C.POINTER(C.c_double)
+_I32P = C.POINTER(C.c_int32)
+_U32P = C.POINTER(C.c_uint32)
+_I64P = C.POINTER(C.c_int64)
+_VP = C.c_void_p
+
+# Every symbol the header declares, with its ctypes signature (restype, argtypes).
+SIGNATURES = {
+    "cuscan_version": (C.c_char_p, []),
+    "cuscan_launch_count": (C.c_int64, []),
+    "cuscan_ctx_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "cuscan_ctx_destroy": (None, [_VP]),
+    "cuscan_last_error": (C.c_char_p, [_VP]),
+    "cuscan_error_kind": (C.c_int, [_VP]),
+    "cuscan_ctx_stream": (_VP, [_VP]),
+    "cuscan_exact_knn": (C.c_int, [_VP, _VP, C.c_int64, _VP, C.c_int64, C.c_int32, C.c_int32,
+                                   C.c_int32, C.c_int64, C.c_int32, _VP, _VP, _VP]),
+    "cuscan_boruvka_candidates": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int64, C.c_int32, _VP, _VP,
+                                            _VP]),
+    "cuscan_component_reduce": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int64,
+                                          C.c_int64, C.c_int64, _VP, _VP, _VP]),
+    "cuscan_fit_core": (C.c_int, [_VP, _F32P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _I32P,
+                                  _F32P, _F32P, _U32P, _U32P, _F32P, _I64P, _VP]),
+    "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                         _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
+    "cuscan_clusters_from_spanning_tree": (C.c_int, [_U32P, _U32P, _F64P, C.c_int64, _VP,
+                                                     C.POINTER(_VP), C.c_char_p, C.c_size_t]),
+    "cuscan_clustering_points": (C.c_int64, [_VP]),
+    "cuscan_clustering_condensed_rows": (C.c_int64, [_VP]),
+    "cuscan_clustering_read": (None, [_VP, _I32P, _F32P, _F64P, _F64P, _I64P, _I64P, _F32P,
+                                      _F32P]),
+    "cuscan_clustering_free": (None, [_VP]),
+    "cuscan_dbscan_cut": (C.c_int, [_F64P, C.c_int64, C.c_double, C.c_int64, _I32P]),
+}
+
+
+class FitStats(C.Structure):
+    _fields_ = [
+        ("core_ms", C.c_double),
+        ("mst_ms", C.c_double),
+        ("knn_kernel_ms", C.c_double),
+        ("candidate_kernel_ms", C.c_double),
+        ("rounds", C.c_int64),
+        ("seed_edges", C.c_int64),
+        ("components_after_seed", C.c_int64),
+        ("refined_rows", C.c_int64),
+        ("fallback_rows", C.c_int64),
+        ("cross_pairs", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ExtractConfig(C.Structure):
+    _fields_ = [
+        ("min_cluster_size", C.c_int64),
+        ("selection_leaf", C.c_int32),
+        ("allow_single_cluster", C.c_int32),
+        ("max_cluster_size", C.c_int64),
+        ("cluster_selection_epsilon", C.c_double),
+        ("cluster_selection_persistence", C.c_double),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "_build" / "libcuscan_gb300.so"
+
+
+def load(build_if_missing: bool = True):
+    """Load the shared library (building it first when it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not path.exists() and build_if_missing:
+            from . import build as _build
+            _build.build()
+        if not path.exists():
+            raise RuntimeError(f"cuscan_gb300 native library is missing: {path}")
+        lib = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process so far."""
+    return int(load().cuscan_launch_count())
+
+
+def raise_for(code: int, message: str):
+    if code == OK:
+        return
+    if code in (INVALID_CONFIG, INVALID_INPUT):
+        raise ValueError(message)
+    if code in (BACKEND_UNAVAILABLE, NUMERICAL):
+        raise RuntimeError(message)
+    if code in (OVERFLOW, CAPACITY):
+        raise OverflowError(message)
+    if code == MEMORY:
+        raise MemoryError(message)
+    raise RuntimeError(f"cuscan_gb300 status {code}: {message}")
+
+
+class Context:
+    """One CUDA device context of the library (its own stream and reusable workspace)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        handle = _VP()
+        code = self._lib.cuscan_ctx_create(int(device), C.byref(handle))
+        if code != OK:
+            raise_for(BACKEND_UNAVAILABLE if code == BACKEND_UNAVAILABLE else code,
+                      f"CUDA device {device} is unavailable (a Blackwell-class device is required)")
+        self.handle = handle
+        self.device = int(device)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.cuscan_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.cuscan_ctx_stream(self.handle) or 0)
+
+    def check(self, code: int):
+        if code != OK:
+            msg = self._lib.cuscan_last_error(self.handle).decode("utf-8", "replace")
+            raise_for(code, msg)
+
+    # ---- backend operations on device pointers (integers) ----
+    def exact_knn(self, query, nq, reference, nr, d, k, exclude_self, query_offset, squared,
+                  ids_out, dist_out, stream=None):
+        self.check(self._lib.cuscan_exact_knn(self.handle, query, nq, reference, nr, d, k,
+                                              int(exclude_self), query_offset, int(squared),
+                                              ids_out, dist_out, stream))
+
+    def boruvka_candidates(self, data, core_sq, components, n, d, weights_out, dst_out,
+                           stream=None):
+        self.check(self._lib.cuscan_boruvka_candidates(self.handle, data, core_sq, components, n,
+                                                       d, weights_out, dst_out, stream))
+
+    def component_reduce(self, weights, indices, members, tile_starts, tile_ends,
+                         partial_offsets, n, p, c, win_weights, win_meta, stream=None):
+        self.check(self._lib.cuscan_component_reduce(self.handle, weights, indices, members,
+                                                     tile_starts, tile_ends, partial_offsets, n,
+                                                     p, c, win_weights, win_meta, stream))
+
+    def fit_core_device(self, data, n, d, min_samples, precision, knn_ids, knn_sq, core_sq,
+                        src, dst, wsq, stream=None):
+        m = C.c_int64(0)
+        stats = FitStats()
+        self.check(self._lib.cuscan_fit_core_device(self.handle, data, n, d, min_samples,
+                                                    precision, knn_ids, knn_sq, core_sq, src,
+                                                    dst, wsq, C.byref(m), C.byref(stats), stream))
+        return int(m.value), stats
+
+    # ---- host-pointer fit ----
+    def fit_core(self, x: np.ndarray, min_samples: int, precision: int = PRECISION_PLAIN):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n, d = x.shape
+        k = min(int(min_samples), n - 1)
+        ids = np.empty((n, k), np.int32)
+        ksq = np.empty((n, k), np.float32)
+        core = np.empty(n, np.float32)
+        src = np.empty(max(n - 1, 1), np.uint32)
+        dst = np.empty(max(n - 1, 1), np.uint32)
+        w = np.empty(max(n - 1, 1), np.float32)
+        m = C.c_int64(0)
+        stats = FitStats()
+        self.check(self._lib.cuscan_fit_core(
+            self.handle, x.ctypes.data_as(_F32P), n, d, int(min_samples), int(precision),
+            ids.ctypes.data_as(_I32P), ksq.ctypes.data_as(_F32P), core.ctypes.data_as(_F32P),
+            src.ctypes.data_as(_U32P), dst.ctypes.data_as(_U32P), w.ctypes.data_as(_F32P),
+            C.byref(m), C.byref(stats)))
+        e = int(m.value)
+        return {"knn_ids": ids, "knn_sq": ksq, "core_sq": core, "src": src[:e], "dst": dst[:e],
+                "wsq": w[:e], "stats": stats.as_dict()}
+
+
+def clusters_from_spanning_tree(src, dst, weight, *, min_cluster_size: int,
+                                cluster_selection_method: str = "eom",
+                                allow_single_cluster: bool = False,
+                                max_cluster_size: int | None = None,
+                                cluster_selection_epsilon: float = 0.0,
+                                cluster_selection_persistence: float = 0.0) -> dict:
+    """Host extraction of labels, strengths, linkage and condensed tree from an MST."""
+    lib = load()
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    weight = np.ascontiguousarray(weight, np.float64)
+    m = int(src.shape[0])
+    cfg = ExtractConfig(int(min_cluster_size), 1 if cluster_selection_method == "leaf" else 0,
+                        1 if allow_single_cluster else 0,
+                        0 if max_cluster_size is None else int(max_cluster_size),
+                        float(cluster_selection_epsilon), float(cluster_selection_persistence))
+    out = _VP()
+    err = C.create_string_buffer(512)
+    code = lib.cuscan_clusters_from_spanning_tree(
+        src.ctypes.data_as(_U32P), dst.ctypes.data_as(_U32P), weight.ctypes.data_as(_F64P), m,
+        C.byref(cfg), C.byref(out), err, 512)
+    raise_for(code, err.value.decode("utf-8", "replace"))
+    try:
+        npts = int(lib.cuscan_clustering_points(out))
+        rows = int(lib.cuscan_clustering_condensed_rows(out))
+        labels = np.empty(npts, np.int32)
+        prob = np.empty(npts, np.float32)
+        linkage = np.empty((m, 4), np.float64)
+        smst = np.empty((m, 3), np.float64)
+        cp = np.empty(rows, np.int64)
+        cc = np.empty(rows, np.int64)
+        cl = np.empty(rows, np.float32)
+        cs = np.empty(rows, np.float32)
+        lib.cuscan_clustering_read(out, labels.ctypes.data_as(_I32P), prob.ctypes.data_as(_F32P),
+                                   linkage.ctypes.data_as(_F64P), smst.ctypes.data_as(_F64P),
+                                   cp.ctypes.data_as(_I64P), cc.ctypes.data_as(_I64P),
+                                   cl.ctypes.data_as(_F32P), cs.ctypes.data_as(_F32P))
+    finally:
+        lib.cuscan_clustering_free(out)
+    return {"labels": labels, "probabilities": prob, "linkage": linkage, "sorted_mst": smst,
+            "condensed_parent": cp, "condensed_child": cc, "condensed_lambda": cl,
+            "condensed_child_size": cs}
+
+
+def dbscan_cut(linkage: np.ndarray, cut: float, min_size: int) -> np.ndarray:
+    lib = load()
+    linkage = np.ascontiguousarray(linkage, np.float64)
+    rows = int(linkage.shape[0])
+    out = np.empty(rows + 1, np.int32)
+    code = lib.cuscan_dbscan_cut(linkage.ctypes.data_as(_F64P), rows, float(cut), int(min_size),
+                                 out.ctypes.data_as(_I32P))
+    raise_for(code, "DBSCAN cut must not be NaN" if code == INVALID_CONFIG else "invalid linkage")
+    return out

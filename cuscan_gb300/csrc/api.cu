@@ -1,0 +1,327 @@
+// C ABI of cuscan_gb300: context management, the three backend operations and the fused
+// device-resident fit core.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "forest.cuh"
+
+namespace cuscan {
+
+struct FitWorkspace {
+    ForestBuffers forest;
+    Buffer x, ids, dsq, core, label, src, dst, w;  // device copies for the host-pointer entry
+    Buffer op_keys, op_tiles_lo, op_tiles_hi, op_partials, op_knn_ids, op_knn_dist;
+    DevStatus *host_status = nullptr;              // pinned
+    cudaEvent_t ev[6] = {};
+};
+
+// Refined (bf16 tensor-core) sweeps; defined in refined.cu.
+int refined_available();
+int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d, int k,
+                       int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
+                       int64_t *fallback_rows);
+int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
+                              cudaStream_t s, int64_t *refined_rows);
+
+}  // namespace cuscan
+
+using namespace cuscan;
+
+extern "C" {
+
+const char *cuscan_version(void) { return "cuscan_gb300 0.1.0 (sm_103a)"; }
+
+int64_t cuscan_launch_count(void) { return (int64_t)launch_counter().load(); }
+
+int cuscan_ctx_create(int device, cuscan_ctx **out) {
+    if (!out) return CUSCAN_INVALID_INPUT;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return CUSCAN_BACKEND_UNAVAILABLE;
+    }
+    if (device < 0 || device >= count) return CUSCAN_BACKEND_UNAVAILABLE;
+    cuscan_ctx *ctx = new cuscan_ctx();
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return CUSCAN_BACKEND_UNAVAILABLE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
+        ctx->sm_count = prop.multiProcessorCount;
+        if (prop.major < 10) {
+            cudaStreamDestroy(ctx->stream);
+            delete ctx;
+            return CUSCAN_BACKEND_UNAVAILABLE;
+        }
+    }
+    ctx->fit = new FitWorkspace();
+    if (cudaMallocHost(&ctx->fit->host_status, sizeof(DevStatus)) != cudaSuccess) {
+        cudaGetLastError();
+        cuscan_ctx_destroy(ctx);
+        return CUSCAN_MEMORY;
+    }
+    for (auto &ev : ctx->fit->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return CUSCAN_OK;
+}
+
+void cuscan_ctx_destroy(cuscan_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->fit) {
+        FitWorkspace *f = ctx->fit;
+        forest_release(f->forest);
+        Buffer *all[] = {&f->x, &f->ids, &f->dsq, &f->core, &f->label, &f->src, &f->dst, &f->w,
+                         &f->op_keys, &f->op_tiles_lo, &f->op_tiles_hi, &f->op_partials,
+                         &f->op_knn_ids, &f->op_knn_dist};
+        for (Buffer *b : all) release(*b);
+        if (f->host_status) cudaFreeHost(f->host_status);
+        for (auto &ev : f->ev)
+            if (ev) cudaEventDestroy(ev);
+        delete f;
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *cuscan_last_error(const cuscan_ctx *ctx) { return ctx ? ctx->err : "null context"; }
+int cuscan_error_kind(const cuscan_ctx *ctx) { return ctx ? ctx->kind : CUSCAN_INVALID_INPUT; }
+void *cuscan_ctx_stream(cuscan_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int cuscan_exact_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *reference,
+                     int64_t nr, int32_t d, int32_t k, int32_t exclude_self,
+                     int64_t query_offset, int32_t squared, int32_t *ids_out, float *dist_out,
+                     void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (nq < 0 || nr <= 0 || d <= 0 || k <= 0)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "exact_knn needs nq >= 0, nr > 0, d > 0, k > 0");
+    if (nr > INT32_MAX - 1 || nq > INT32_MAX)
+        return fail(ctx, CUSCAN_OVERFLOW, "row count exceeds the supported integer range");
+    if (nq > 0 && (!query || !reference || !ids_out || !dist_out))
+        return fail(ctx, CUSCAN_INVALID_INPUT, "exact_knn received a null pointer");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    return launch_exact_knn_fp32(ctx, query, nq, reference, nr, d, k, exclude_self, query_offset,
+                                 squared, ids_out, dist_out, pick_stream(ctx, stream),
+                                 ctx->fit->op_knn_ids, ctx->fit->op_knn_dist);
+}
+
+int cuscan_boruvka_candidates(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                              const int32_t *components, int64_t n, int32_t d, float *weights_out,
+                              int32_t *destinations_out, void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n <= 0 || d <= 0)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "Boruvka candidate input must contain at least one row");
+    if (n > INT32_MAX - 1) return fail(ctx, CUSCAN_OVERFLOW, "Boruvka row indices");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    FitWorkspace *f = ctx->fit;
+    int rc = ensure(ctx, f->op_keys, sizeof(unsigned long long) * n, "candidate keys");
+    if (!rc) rc = ensure(ctx, f->op_tiles_lo, sizeof(int32_t) * (ceil_div(n, 32) + 1), "tiles");
+    if (!rc) rc = ensure(ctx, f->op_tiles_hi, sizeof(int32_t) * (ceil_div(n, 32) + 1), "tiles");
+    if (rc) return rc;
+    unsigned long long *keys = as<unsigned long long>(f->op_keys);
+    if ((rc = launch_fill_u64(ctx, keys, n, ~0ull, s))) return rc;
+    if ((rc = launch_candidates_fp32(ctx, data, core_sq, components, nullptr, n, d, keys,
+                                     as<int32_t>(f->op_tiles_lo), as<int32_t>(f->op_tiles_hi), s)))
+        return rc;
+    return launch_keys_to_candidates(ctx, keys, n, weights_out, destinations_out, s);
+}
+
+int cuscan_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t *indices,
+                            const int32_t *members, const int32_t *tile_starts,
+                            const int32_t *tile_ends, const int32_t *partial_offsets, int64_t n,
+                            int64_t p, int64_t c, float *win_weights, int32_t *win_meta,
+                            void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n < 0 || p < 0 || c < 0 || c > n || p > n)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "component_reduce received inconsistent sizes");
+    if (n > INT32_MAX) return fail(ctx, CUSCAN_OVERFLOW, "component member index");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    return launch_component_reduce(ctx, weights, indices, members, tile_starts, tile_ends,
+                                   partial_offsets, n, p, c, win_weights, win_meta,
+                                   ctx->fit->op_partials, pick_stream(ctx, stream));
+}
+
+static int read_status(cuscan_ctx *ctx, DevStatus *dev, DevStatus *host, cudaStream_t s) {
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(host, dev, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    return CUSCAN_OK;
+}
+
+static int status_error(cuscan_ctx *ctx, int kind) {
+    switch (kind) {
+        case 1:
+            return fail(ctx, CUSCAN_NUMERICAL,
+                        "Boruvka candidate weight must be nonnegative and not NaN");
+        case 2:
+            return fail(ctx, CUSCAN_INVALID_INPUT, "candidate index is out of range");
+        default:
+            return fail(ctx, CUSCAN_NUMERICAL, "Boruvka round made no progress");
+    }
+}
+
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                           int32_t min_samples, int32_t precision, int32_t *knn_ids,
+                           float *knn_sq, float *core_sq, uint32_t *mst_src, uint32_t *mst_dst,
+                           float *mst_wsq, int64_t *n_edges, cuscan_fit_stats *stats,
+                           void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n_edges) *n_edges = 0;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (min_samples <= 0) return fail(ctx, CUSCAN_INVALID_CONFIG, "min_samples must be positive");
+    if (n < 2 || d <= 0)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "the fit core needs at least two rows and one feature");
+    if (n > INT32_MAX - 1)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "row count %lld exceeds the supported maximum",
+                    (long long)n);
+    if (precision != CUSCAN_PRECISION_PLAIN && precision != CUSCAN_PRECISION_BF16_REFINED)
+        return fail(ctx, CUSCAN_INVALID_CONFIG, "unknown precision %d", precision);
+    if (precision == CUSCAN_PRECISION_BF16_REFINED && !refined_available())
+        return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE,
+                    "bf16-refined sweeps are not available for this shape");
+    if (!data || !knn_ids || !knn_sq || !core_sq || !mst_src || !mst_dst || !mst_wsq)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "fit_core_device received a null pointer");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    FitWorkspace *f = ctx->fit;
+    ForestBuffers &b = f->forest;
+    int rc = forest_reserve(ctx, b, n, d);
+    if (!rc) rc = ensure(ctx, f->label, sizeof(int32_t) * n, "point labels");
+    if (rc) return rc;
+    const int k = (int)((int64_t)min_samples < n - 1 ? min_samples : n - 1);
+    int32_t *label = as<int32_t>(f->label);
+    cudaEvent_t *ev = f->ev;
+    int64_t refined_rows = 0, fallback_rows = 0;
+
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
+    CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
+    // ---- core_distances: exact kNN sweep (estimator.rs:591-657) + core column ----
+    if (precision == CUSCAN_PRECISION_BF16_REFINED)
+        rc = launch_knn_refined(ctx, b, data, n, d, k, knn_ids, knn_sq, s, &refined_rows,
+                                &fallback_rows);
+    else
+        rc = launch_exact_knn_fp32(ctx, data, n, data, n, d, k, 1, 0, 1, knn_ids, knn_sq, s,
+                                   b.knn_ids_tmp, b.knn_dist_tmp);
+    if (rc) return rc;
+    CUSCAN_CUDA(ctx, cudaEventRecord(ev[1], s));
+    if ((rc = forest_core(ctx, knn_sq, n, k, min_samples, core_sq, s))) return rc;
+    CUSCAN_CUDA(ctx, cudaEventRecord(ev[2], s));
+    // ---- mst: kNN seed then Borůvka rounds (estimator.rs:689-874) ----
+    if ((rc = forest_seed(ctx, b, core_sq, knn_ids, knn_sq, n, k, label, mst_src, mst_dst,
+                          mst_wsq, s)))
+        return rc;
+    DevStatus *hs = f->host_status;
+    if ((rc = read_status(ctx, b.status, hs, s))) return rc;
+    if (hs->err_kind) return status_error(ctx, hs->err_kind);
+    const int64_t seed_edges = (int64_t)hs->edges;
+    const int64_t after_seed = (int64_t)hs->components;
+    int64_t components = (int64_t)hs->components;
+    int64_t rounds = 0;
+    double cand_ms = 0.0, cross_pairs = 0.0;
+    while (components > 1) {
+        if (rounds > 64) return fail(ctx, CUSCAN_NUMERICAL, "Boruvka did not converge");
+        if ((rc = forest_sort_by_component(ctx, b, data, core_sq, label, n, d, s))) return rc;
+        unsigned long long *row_keys = as<unsigned long long>(b.row_keys);
+        if ((rc = launch_fill_u64(ctx, row_keys, n, ~0ull, s))) return rc;
+        CUSCAN_CUDA(ctx, cudaEventRecord(ev[4], s));
+        if (precision == CUSCAN_PRECISION_BF16_REFINED)
+            rc = launch_candidates_refined(ctx, b, n, d, s, &refined_rows);
+        else
+            rc = launch_candidates_fp32(ctx, as<float>(b.xp), as<float>(b.corep),
+                                        as<int32_t>(b.labp), as<int32_t>(b.perm), n, d, row_keys,
+                                        as<int32_t>(b.tile_lo), as<int32_t>(b.tile_hi), s);
+        if (rc) return rc;
+        CUSCAN_CUDA(ctx, cudaEventRecord(ev[5], s));
+        if ((rc = forest_round(ctx, b, n, components, label, mst_src, mst_dst, mst_wsq, s)))
+            return rc;
+        if ((rc = read_status(ctx, b.status, hs, s))) return rc;
+        cand_ms += elapsed(ev[4], ev[5]);
+        cross_pairs += (double)n * (double)n - hs->same_pairs;
+        if (hs->err_kind) return status_error(ctx, hs->err_kind);
+        ++rounds;
+        components = (int64_t)hs->components;
+    }
+    CUSCAN_CUDA(ctx, cudaEventRecord(ev[3], s));
+    CUSCAN_CUDA(ctx, cudaEventSynchronize(ev[3]));
+    if ((int64_t)hs->edges != n - 1)
+        return fail(ctx, CUSCAN_NUMERICAL, "Boruvka produced an incomplete spanning tree");
+    if (n_edges) *n_edges = (int64_t)hs->edges;
+    if (stats) {
+        stats->core_ms = elapsed(ev[0], ev[2]);
+        stats->mst_ms = elapsed(ev[2], ev[3]);
+        stats->knn_kernel_ms = elapsed(ev[0], ev[1]);
+        stats->candidate_kernel_ms = cand_ms;
+        stats->rounds = rounds;
+        stats->seed_edges = seed_edges;
+        stats->components_after_seed = after_seed;
+        stats->refined_rows = refined_rows;
+        stats->fallback_rows = fallback_rows;
+        stats->cross_pairs = cross_pairs;
+    }
+    return CUSCAN_OK;
+}
+
+int cuscan_fit_core(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                    int32_t min_samples, int32_t precision, int32_t *knn_ids, float *knn_sq,
+                    float *core_sq, uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                    int64_t *n_edges, cuscan_fit_stats *stats) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (min_samples <= 0) return fail(ctx, CUSCAN_INVALID_CONFIG, "min_samples must be positive");
+    if (n < 2 || d <= 0)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "the fit core needs at least two rows and one feature");
+    if (!data || !core_sq || !mst_src || !mst_dst || !mst_wsq)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "fit_core received a null pointer");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    FitWorkspace *f = ctx->fit;
+    cudaStream_t s = ctx->stream;
+    const int64_t k = (int64_t)min_samples < n - 1 ? min_samples : n - 1;
+    int rc = ensure(ctx, f->x, sizeof(float) * n * d, "input rows");
+    if (!rc) rc = ensure(ctx, f->ids, sizeof(int32_t) * n * k, "kNN ids");
+    if (!rc) rc = ensure(ctx, f->dsq, sizeof(float) * n * k, "kNN distances");
+    if (!rc) rc = ensure(ctx, f->core, sizeof(float) * n, "core distances");
+    if (!rc) rc = ensure(ctx, f->src, sizeof(uint32_t) * n, "MST sources");
+    if (!rc) rc = ensure(ctx, f->dst, sizeof(uint32_t) * n, "MST destinations");
+    if (!rc) rc = ensure(ctx, f->w, sizeof(float) * n, "MST weights");
+    if (rc) return rc;
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(f->x.ptr, data, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+    int64_t m = 0;
+    rc = cuscan_fit_core_device(ctx, as<float>(f->x), n, d, min_samples, precision,
+                                as<int32_t>(f->ids), as<float>(f->dsq), as<float>(f->core),
+                                as<uint32_t>(f->src), as<uint32_t>(f->dst), as<float>(f->w), &m,
+                                stats, s);
+    if (rc) return rc;
+    if (knn_ids)
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(knn_ids, f->ids.ptr, sizeof(int32_t) * n * k,
+                                         cudaMemcpyDeviceToHost, s));
+    if (knn_sq)
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(knn_sq, f->dsq.ptr, sizeof(float) * n * k,
+                                         cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(core_sq, f->core.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(mst_src, f->src.ptr, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(mst_dst, f->dst.ptr, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(mst_wsq, f->w.ptr, sizeof(float) * m, cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    if (n_edges) *n_edges = m;
+    return CUSCAN_OK;
+}
+
+}  // extern "C"

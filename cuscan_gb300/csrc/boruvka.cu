@@ -1,0 +1,356 @@
+// Borůvka round kernels with f32 direct differences (the "plain" arithmetic), and the CSR
+// component reduction of the reference's HdbscanOps::component_reduce.
+//
+// Candidate rule (crates/hdbscan/src/kernels/boruvka.rs:68-140): for row i, the
+// lexicographically smallest (w_ij, j) with w_ij = max(max(d2_ij, core_i), core_j) over rows j
+// of another component. Here a (w, j) pair is packed into one 64-bit key
+// (canonical weight bits << 32 | j): for non-negative weights the unsigned key order is exactly
+// that lexicographic order, so partial results from any split of the reference range combine
+// with a single atomicMin.
+//
+// The fused fit path calls the kernel on component-sorted rows. A (query block, reference
+// tile) pair whose rows all carry one label holds only same-component pairs and is skipped
+// before any distance is computed; tile label ranges are precomputed per 32-row tile.
+#include "common.cuh"
+
+namespace cuscan {
+namespace {
+
+constexpr int QB = 128;
+constexpr int RT = 32;
+constexpr int RTP = 36;
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, bool valid) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    int src_size = valid ? 4 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(src_size));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Label range of each RT-row tile.
+__global__ void tile_range_kernel(const int32_t *__restrict__ labels, int64_t n,
+                                  int32_t *__restrict__ lo, int32_t *__restrict__ hi) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t tiles = ceil_div(n, RT);
+    if (t >= tiles) return;
+    int64_t a = t * RT, b = a + RT < n ? a + RT : n;
+    int32_t mn = labels[a], mx = labels[a];
+    for (int64_t i = a + 1; i < b; ++i) {
+        int32_t l = labels[i];
+        mn = l < mn ? l : mn;
+        mx = l > mx ? l : mx;
+    }
+    lo[t] = mn;
+    hi[t] = mx;
+}
+
+__device__ __forceinline__ void load_tile(float *tile, float *core_t, int32_t *lab_t,
+                                          int32_t *id_t, const float *data, const float *core,
+                                          const int32_t *labels, const int32_t *ids, int64_t n,
+                                          int d, int64_t r0) {
+    const int total = RT * d;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        int r = e / d;
+        int f = e - r * d;
+        int64_t row = r0 + r;
+        bool valid = row < n;
+        cp_async4(&tile[f * RTP + r], valid ? data + row * (int64_t)d + f : data, valid);
+    }
+    if (threadIdx.x < RT) {
+        int64_t row = r0 + threadIdx.x;
+        bool valid = row < n;
+        core_t[threadIdx.x] = valid ? core[row] : 0.0f;
+        lab_t[threadIdx.x] = valid ? labels[row] : -1;
+        id_t[threadIdx.x] = valid ? (ids ? ids[row] : (int32_t)row) : -1;
+    }
+}
+
+__global__ void __launch_bounds__(QB) candidates_fp32_kernel(
+    const float *__restrict__ data, const float *__restrict__ core,
+    const int32_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n, int d,
+    const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t ref_chunk,
+    unsigned long long *__restrict__ row_keys) {
+    extern __shared__ __align__(16) float smem[];
+    float *qs = smem;                       // [d][QB]
+    float *tiles = smem + (size_t)d * QB;   // 2 x [d][RTP]
+    __shared__ float core_t[2][RT];
+    __shared__ int32_t lab_t[2][RT];
+    __shared__ int32_t id_t[2][RT];
+    const int tid = threadIdx.x;
+    const int64_t q0 = (int64_t)blockIdx.x * QB;
+    const int64_t qi = q0 + tid;
+    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
+    int64_t r_end = r_begin + ref_chunk;
+    if (r_end > n) r_end = n;
+
+    // label range of this block's queries (QB = 4 tiles)
+    int32_t qlo = INT32_MAX, qhi = INT32_MIN;
+    for (int t = 0; t < QB / RT; ++t) {
+        int64_t tt = q0 / RT + t;
+        if (tt * RT < n) {
+            qlo = min(qlo, tile_lo[tt]);
+            qhi = max(qhi, tile_hi[tt]);
+        }
+    }
+    const bool q_uniform = qlo == qhi;
+
+    for (int e = tid; e < QB * d; e += QB) {
+        int q = e / d;
+        int f = e - q * d;
+        int64_t row = q0 + q;
+        qs[f * QB + q] = row < n ? data[row * (int64_t)d + f] : 0.0f;
+    }
+    const bool q_valid = qi < n;
+    const int32_t my_label = q_valid ? labels[qi] : -1;
+    const float my_core = q_valid ? core[qi] : 0.0f;
+    unsigned long long best = ~0ull;
+
+    auto skip_tile = [&](int64_t r0) -> bool {
+        int64_t t = r0 / RT;
+        return q_uniform && tile_lo[t] == qlo && tile_hi[t] == qlo;
+    };
+    auto next_tile = [&](int64_t r0) -> int64_t {
+        while (r0 < r_end && skip_tile(r0)) r0 += RT;
+        return r0;
+    };
+
+    const int tile_floats = d * RTP;
+    int buf = 0;
+    int64_t r0 = next_tile(r_begin);
+    if (r0 < r_end) {
+        load_tile(tiles, core_t[0], lab_t[0], id_t[0], data, core, labels, ids, r_end, d, r0);
+        cp_async_commit();
+    }
+    while (r0 < r_end) {
+        const int64_t nxt = next_tile(r0 + RT);
+        if (nxt < r_end) {
+            load_tile(tiles + (buf ^ 1) * tile_floats, core_t[buf ^ 1], lab_t[buf ^ 1],
+                      id_t[buf ^ 1], data, core, labels, ids, r_end, d, nxt);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const float *tile = tiles + buf * tile_floats;
+        float acc[RT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) acc[r] = 0.0f;
+        const float *qcol = qs + tid;
+#pragma unroll 2
+        for (int f = 0; f < d; ++f) {
+            const float qv = qcol[f * QB];
+            const float4 *row4 = reinterpret_cast<const float4 *>(tile + f * RTP);
+#pragma unroll
+            for (int r4 = 0; r4 < RT / 4; ++r4) {
+                const float4 v = row4[r4];
+                float t0 = qv - v.x, t1 = qv - v.y, t2 = qv - v.z, t3 = qv - v.w;
+                acc[4 * r4 + 0] = __fmaf_rn(t0, t0, acc[4 * r4 + 0]);
+                acc[4 * r4 + 1] = __fmaf_rn(t1, t1, acc[4 * r4 + 1]);
+                acc[4 * r4 + 2] = __fmaf_rn(t2, t2, acc[4 * r4 + 2]);
+                acc[4 * r4 + 3] = __fmaf_rn(t3, t3, acc[4 * r4 + 3]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RT; ++r) {
+            const int32_t lj = lab_t[buf][r];
+            if (lj >= 0 && lj != my_label) {
+                float w = fmaxf(fmaxf(acc[r], my_core), core_t[buf][r]);
+                if (!(w != w)) {
+                    unsigned long long key =
+                        ((unsigned long long)weight_key_bits(w) << 32) | (uint32_t)id_t[buf][r];
+                    best = key < best ? key : best;
+                }
+            }
+        }
+        __syncthreads();
+        buf ^= 1;
+        r0 = nxt;
+    }
+    if (q_valid && best != ~0ull) {
+        const int32_t out = ids ? ids[qi] : (int32_t)qi;
+        atomicMin(&row_keys[out], best);
+    }
+}
+
+__global__ void fill_u64_kernel(unsigned long long *p, int64_t n, unsigned long long v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+__global__ void keys_to_candidates_kernel(const unsigned long long *__restrict__ keys, int64_t n,
+                                          float *__restrict__ w, int32_t *__restrict__ dst) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    unsigned long long k = keys[i];
+    if (k == ~0ull) {
+        w[i] = CUSCAN_INF;
+        dst[i] = (int32_t)n;
+    } else {
+        w[i] = __uint_as_float((uint32_t)(k >> 32));
+        dst[i] = (int32_t)(uint32_t)k;
+    }
+}
+
+// ---- CSR component reduction (component_reduce.rs semantics) ----
+
+struct Fold {
+    uint32_t key, bits, source, bad;
+};
+
+__device__ __forceinline__ void fold_take(Fold &a, const Fold &b) {
+    if (b.key < a.key || (b.key == a.key && b.source < a.source)) {
+        a.key = b.key;
+        a.bits = b.bits;
+        a.source = b.source;
+    }
+    a.bad = b.bad < a.bad ? b.bad : a.bad;
+}
+
+__device__ __forceinline__ Fold warp_fold(Fold v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Fold u;
+        u.key = __shfl_xor_sync(0xffffffffu, v.key, o);
+        u.bits = __shfl_xor_sync(0xffffffffu, v.bits, o);
+        u.source = __shfl_xor_sync(0xffffffffu, v.source, o);
+        u.bad = __shfl_xor_sync(0xffffffffu, v.bad, o);
+        fold_take(v, u);
+    }
+    return v;
+}
+
+// One warp per tile of CSR positions [tile_starts[t], tile_ends[t]).
+__global__ void reduce_tiles_kernel(const float *__restrict__ weights,
+                                    const int32_t *__restrict__ indices,
+                                    const int32_t *__restrict__ members,
+                                    const int32_t *__restrict__ starts,
+                                    const int32_t *__restrict__ ends, int64_t p, uint32_t n,
+                                    Fold *__restrict__ partial) {
+    int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    int lane = threadIdx.x & 31;
+    if (t >= p) return;
+    Fold acc{0xffffffffu, 0x7f800000u, n, n};
+    for (int64_t pos = starts[t] + lane; pos < ends[t]; pos += 32) {
+        uint32_t member = (uint32_t)members[pos];
+        uint32_t original = __float_as_uint(weights[member]);
+        int32_t destination = indices[member];
+        Fold v{0xffffffffu, 0x7f800000u, n, n};
+        if (numerical_bits(original) || destination >= (int32_t)n) {
+            v.bad = member;
+        } else if (destination >= 0) {
+            v.key = (original & 0x7fffffffu) == 0 ? 0u : original;
+            v.bits = original;
+            v.source = member;
+        }
+        fold_take(acc, v);
+    }
+    acc = warp_fold(acc);
+    if (lane == 0) partial[t] = acc;
+}
+
+// One warp per component over its tile partials; writes winner weight and 5-int metadata.
+__global__ void reduce_components_kernel(const float *__restrict__ weights,
+                                         const int32_t *__restrict__ indices,
+                                         const int32_t *__restrict__ partial_offsets,
+                                         const Fold *__restrict__ partial, int64_t c, uint32_t n,
+                                         float *__restrict__ win_w, int32_t *__restrict__ win_meta) {
+    int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    int lane = threadIdx.x & 31;
+    if (s >= c) return;
+    Fold acc{0xffffffffu, 0x7f800000u, n, n};
+    for (int64_t t = partial_offsets[s] + lane; t < partial_offsets[s + 1]; t += 32)
+        fold_take(acc, partial[t]);
+    acc = warp_fold(acc);
+    if (lane != 0) return;
+    int32_t destination = acc.source < n ? indices[acc.source] : -1;
+    int32_t kind = 0, bad_destination = -1;
+    if (acc.bad < n) {
+        if (numerical_bits(__float_as_uint(weights[acc.bad]))) {
+            kind = 1;
+        } else {
+            kind = 2;
+            bad_destination = indices[acc.bad];
+        }
+    }
+    win_w[s] = __uint_as_float(acc.bits);
+    int32_t *m = win_meta + s * 5;
+    m[0] = acc.source < n ? (int32_t)acc.source : -1;
+    m[1] = destination;
+    m[2] = (int32_t)acc.bad;
+    m[3] = kind;
+    m[4] = bad_destination;
+}
+
+}  // namespace
+
+int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                           const int32_t *labels, const int32_t *ids, int64_t n, int d,
+                           unsigned long long *row_keys, int32_t *tile_lo, int32_t *tile_hi,
+                           cudaStream_t s) {
+    const int64_t tiles = ceil_div(n, RT);
+    CUSCAN_KERNEL(tile_range_kernel, (unsigned)ceil_div(tiles, 256), 256, 0, s, labels, n, tile_lo, tile_hi);
+    CUSCAN_LAUNCH(ctx, "tile_range_kernel");
+    const int64_t qblocks = ceil_div(n, QB);
+    int64_t splits = 1;
+    const int64_t target = 2 * (int64_t)ctx->sm_count;
+    if (qblocks < target) splits = ceil_div(target, qblocks);
+    const int64_t max_splits = ceil_div(n, (int64_t)RT * 8);
+    if (splits > max_splits) splits = max_splits;
+    if (splits > 64) splits = 64;
+    if (splits < 1) splits = 1;
+    int64_t chunk = ceil_div(ceil_div(n, splits), RT) * RT;
+    splits = ceil_div(n, chunk);
+    const size_t smem = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
+    if (smem > 200 * 1024)
+        return fail(ctx, CUSCAN_CAPACITY,
+                    "feature count %d exceeds the shared-memory staging limit of the Boruvka "
+                    "kernel (at most 256 features)", d);
+    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(candidates_fp32_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)qblocks, (unsigned)splits);
+    CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d, tile_lo,
+                                                   tile_hi, chunk, row_keys);
+    CUSCAN_LAUNCH(ctx, "candidates_fp32_kernel");
+    return CUSCAN_OK;
+}
+
+int launch_fill_u64(cuscan_ctx *ctx, unsigned long long *p, int64_t n, unsigned long long v,
+                    cudaStream_t s) {
+    if (n <= 0) return CUSCAN_OK;
+    CUSCAN_KERNEL(fill_u64_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, p, n, v);
+    CUSCAN_LAUNCH(ctx, "fill_u64_kernel");
+    return CUSCAN_OK;
+}
+
+int launch_keys_to_candidates(cuscan_ctx *ctx, const unsigned long long *keys, int64_t n,
+                              float *w, int32_t *dst, cudaStream_t s) {
+    CUSCAN_KERNEL(keys_to_candidates_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, keys, n, w, dst);
+    CUSCAN_LAUNCH(ctx, "keys_to_candidates_kernel");
+    return CUSCAN_OK;
+}
+
+int launch_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t *indices,
+                            const int32_t *members, const int32_t *starts, const int32_t *ends,
+                            const int32_t *partial_offsets, int64_t n, int64_t p, int64_t c,
+                            float *win_w, int32_t *win_meta, Buffer &scratch, cudaStream_t s) {
+    if (c == 0) return CUSCAN_OK;
+    int rc = ensure(ctx, scratch, (size_t)(p > 0 ? p : 1) * sizeof(Fold), "component partials");
+    if (rc) return rc;
+    if (p > 0) {
+        CUSCAN_KERNEL(reduce_tiles_kernel, (unsigned)ceil_div(p * 32, 256), 256, 0, s, 
+            weights, indices, members, starts, ends, p, (uint32_t)n, as<Fold>(scratch));
+        CUSCAN_LAUNCH(ctx, "reduce_tiles_kernel");
+    }
+    CUSCAN_KERNEL(reduce_components_kernel, (unsigned)ceil_div(c * 32, 256), 256, 0, s, 
+        weights, indices, partial_offsets, as<Fold>(scratch), c, (uint32_t)n, win_w, win_meta);
+    CUSCAN_LAUNCH(ctx, "reduce_components_kernel");
+    return CUSCAN_OK;
+}
+
+}  // namespace cuscan

@@ -1,0 +1,529 @@
+// Exact integer work of the MST on the device: the kNN seed forest, per-round component
+// winners, cycle breaking that reproduces the reference's sequential merge order, pointer
+// jumping union/relabel, component sorting and an exclusive scan.
+//
+// Why cycle breaking is enough. In both the seed (crates/hdbscan-core/src/mst.rs:368-420) and
+// a Borůvka merge (mst.rs:259-277) every node (a point, or a component slot) proposes at most
+// one edge, so the proposals form a functional graph: each weakly connected part is a tree
+// (one node without a proposal) or has exactly one cycle. The reference walks the proposals in
+// slot order and skips an edge whose endpoints are already joined. An edge is skipped only if
+// the edges processed before it already connect its endpoints, which closes the part's only
+// cycle, so exactly one edge per cycle is skipped: the cycle edge with the largest slot. Slots
+// are numbered by first appearance, i.e. by the smallest point of a component; components are
+// therefore labelled here by their smallest point, and "largest slot" is "largest label".
+// Pointer doubling with a running maximum finds, for every node, a node on its cycle and the
+// cycle's largest label, without any sequential pass.
+#include "common.cuh"
+#include "forest.cuh"
+
+namespace cuscan {
+namespace {
+
+__device__ __forceinline__ bool active_node(const int32_t *label, int64_t s) {
+    return label == nullptr || label[s] == (int32_t)s;
+}
+
+__global__ void core_kernel(const float *__restrict__ knn_sq, int64_t n, int k, int min_samples,
+                            float *__restrict__ core) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float c;
+    if ((int64_t)min_samples >= n)
+        c = CUSCAN_INF;
+    else if (min_samples == 1)
+        c = 0.0f;
+    else
+        c = knn_sq[i * k + min_samples - 1];
+    core[i] = c;
+}
+
+// Seed proposal of point i: the first non-padding neighbour j with core_i >= core_j
+// (mst.rs:390-417); next[i] = i when there is none.
+__global__ void seed_kernel(const float *__restrict__ core, const int32_t *__restrict__ ids,
+                            const float *__restrict__ dsq, int64_t n, int k,
+                            int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
+                            uint32_t *__restrict__ edst, float *__restrict__ ew,
+                            DevStatus *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float ci = core[i];
+    int32_t pick = (int32_t)i;
+    float w = 0.0f;
+    for (int s = 0; s < k; ++s) {
+        int32_t j = ids[i * k + s];
+        if (j < 0) continue;
+        if ((int64_t)j >= n) {
+            atomicCAS(&status->err_kind, 0, 2);
+            break;
+        }
+        if (ci >= core[j]) {
+            pick = j;
+            w = fmaxf(ci, dsq[i * k + s]);
+            break;
+        }
+    }
+    next[i] = pick;
+    esrc[i] = (uint32_t)i;
+    edst[i] = (uint32_t)pick;
+    ew[i] = w;
+}
+
+__global__ void iota_kernel(int32_t *p, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = (int32_t)i;
+}
+
+__global__ void dbl_init_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ label,
+                                int64_t n, int32_t *__restrict__ jmp, int32_t *__restrict__ mx) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !active_node(label, s)) return;
+    jmp[s] = next[s];
+    mx[s] = (int32_t)s;
+}
+
+__global__ void dbl_step_kernel(const int32_t *__restrict__ jin, const int32_t *__restrict__ min_,
+                                const int32_t *__restrict__ label, int64_t n,
+                                int32_t *__restrict__ jout, int32_t *__restrict__ mout) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !active_node(label, s)) return;
+    int32_t j = jin[s];
+    jout[s] = jin[j];
+    int32_t a = min_[s], b = min_[j];
+    mout[s] = a > b ? a : b;
+}
+
+// keep[s] = s proposes an edge that is not its cycle's largest-label edge; parent[s] is the
+// forest parent after the skipped edges are removed.
+__global__ void keep_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ jmp,
+                            const int32_t *__restrict__ mx, const int32_t *__restrict__ label,
+                            int64_t n, int32_t *__restrict__ keep, int32_t *__restrict__ parent) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    if (!active_node(label, s)) {
+        keep[s] = 0;
+        return;
+    }
+    int32_t t = next[s];
+    bool k = t != (int32_t)s && mx[jmp[s]] != (int32_t)s;
+    keep[s] = k ? 1 : 0;
+    parent[s] = k ? t : (int32_t)s;
+}
+
+__global__ void emit_kernel(const int32_t *__restrict__ keep, const int32_t *__restrict__ pos,
+                            const uint32_t *__restrict__ esrc, const uint32_t *__restrict__ edst,
+                            const float *__restrict__ ew, int64_t n, const DevStatus *status,
+                            uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
+                            float *__restrict__ out_w, int64_t capacity) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !keep[s]) return;
+    int64_t at = (int64_t)status->edges + pos[s];
+    if (at >= capacity) return;
+    out_src[at] = esrc[s];
+    out_dst[at] = edst[s];
+    out_w[at] = ew[s];
+}
+
+__global__ void add_edges_kernel(DevStatus *status, const int32_t *kept_total,
+                                 int require_progress) {
+    status->edges += *kept_total;
+    // "Boruvka round made no progress" (mst.rs:279-283)
+    if (require_progress && *kept_total == 0) atomicCAS(&status->err_kind, 0, 4);
+}
+
+// Path halving toward the root, repeated a fixed number of times by the host.
+__global__ void jump_kernel(int32_t *__restrict__ parent, const int32_t *__restrict__ label,
+                            int64_t n) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !active_node(label, s)) return;
+    int32_t p = parent[s];
+    int32_t pp = parent[p];
+    if (pp != p) parent[s] = pp;
+}
+
+__global__ void minlab_init_kernel(const int32_t *__restrict__ parent,
+                                   const int32_t *__restrict__ label, int64_t n,
+                                   int32_t *__restrict__ minlab) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !active_node(label, s)) return;
+    if (parent[s] == (int32_t)s) minlab[s] = (int32_t)s;
+}
+
+__global__ void minlab_reduce_kernel(const int32_t *__restrict__ parent,
+                                     const int32_t *__restrict__ label, int64_t n,
+                                     int32_t *__restrict__ minlab) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || !active_node(label, s)) return;
+    atomicMin(&minlab[parent[s]], (int32_t)s);
+}
+
+// label[i] <- smallest label of the tree that holds i's old component.
+__global__ void relabel_kernel(int32_t *__restrict__ label, const int32_t *__restrict__ parent,
+                               const int32_t *__restrict__ minlab, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    label[i] = minlab[parent[label[i]]];
+}
+
+__global__ void count_components_kernel(const int32_t *__restrict__ label, int64_t n,
+                                        DevStatus *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool root = i < n && label[i] == (int32_t)i;
+    unsigned m = __ballot_sync(0xffffffffu, root);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(&status->components, (unsigned long long)__popc(m));
+}
+
+// Counting sort of points by label: histogram with warp-aggregated atomics.
+__global__ void hist_kernel(const int32_t *__restrict__ label, int64_t n, int32_t *__restrict__ cnt) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t l = i < n ? label[i] : -1;
+    unsigned peers = __match_any_sync(0xffffffffu, l);
+    int lane = threadIdx.x & 31;
+    if (l >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[l], __popc(peers));
+}
+
+// Sum of squared component sizes (ordered same-component pairs) for the work counters.
+__global__ void same_pairs_kernel(const int32_t *__restrict__ cnt, int64_t n, DevStatus *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < n) {
+        double c = (double)cnt[i];
+        v = c * c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&status->same_pairs, v);
+}
+
+__global__ void scatter_kernel(const int32_t *__restrict__ label, int64_t n,
+                               const int32_t *__restrict__ start, int32_t *__restrict__ fill,
+                               int32_t *__restrict__ perm) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t l = i < n ? label[i] : -1;
+    unsigned peers = __match_any_sync(0xffffffffu, l);
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (l >= 0 && lane == leader) base = atomicAdd(&fill[l], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    if (l < 0) return;
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    perm[start[l] + base + rank] = (int32_t)i;
+}
+
+__global__ void gather_kernel(const float *__restrict__ x, const float *__restrict__ core,
+                              const int32_t *__restrict__ label, const int32_t *__restrict__ perm,
+                              int64_t n, int d, float *__restrict__ xp, float *__restrict__ corep,
+                              int32_t *__restrict__ labp) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * d) return;
+    int64_t pos = e / d;
+    int f = (int)(e - pos * d);
+    int32_t i = perm[pos];
+    xp[e] = x[(int64_t)i * d + f];
+    if (f == 0) {
+        corep[pos] = core[i];
+        labp[pos] = label[i];
+    }
+}
+
+// Per-component minimum of (row weight bits << 32 | row) over component-sorted positions:
+// segmented warp reduction over the contiguous label runs, one atomic per run.
+__global__ void component_min_kernel(const int32_t *__restrict__ perm,
+                                     const int32_t *__restrict__ labp,
+                                     const unsigned long long *__restrict__ row_keys, int64_t n,
+                                     unsigned long long *__restrict__ comp_keys,
+                                     DevStatus *status) {
+    int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int32_t l = -1;
+    unsigned long long v = ~0ull;
+    if (pos < n) {
+        int32_t i = perm[pos];
+        l = labp[pos];
+        unsigned long long rk = row_keys[i];
+        if (rk == ~0ull) {
+            atomicCAS(&status->err_kind, 0, 4);
+        } else {
+            uint32_t wb = (uint32_t)(rk >> 32);
+            if (numerical_bits(wb)) {
+                atomicCAS(&status->err_kind, 0, 1);
+            } else {
+                v = ((unsigned long long)wb << 32) | (uint32_t)i;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long ov = __shfl_down_sync(0xffffffffu, v, o);
+        int32_t ol = __shfl_down_sync(0xffffffffu, l, o);
+        if (lane + o < 32 && ol == l && ov < v) v = ov;
+    }
+    int32_t prev = __shfl_up_sync(0xffffffffu, l, 1);
+    bool head = l >= 0 && (lane == 0 || prev != l);
+    if (head && v != ~0ull) atomicMin(&comp_keys[l], v);
+}
+
+// Winner of each active component: source = argmin row, destination = that row's candidate.
+__global__ void winner_kernel(const int32_t *__restrict__ label,
+                              const unsigned long long *__restrict__ comp_keys,
+                              const unsigned long long *__restrict__ row_keys, int64_t n,
+                              int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
+                              uint32_t *__restrict__ edst, float *__restrict__ ew,
+                              DevStatus *status) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || label[s] != (int32_t)s) return;
+    unsigned long long ck = comp_keys[s];
+    if (ck == ~0ull) {
+        atomicCAS(&status->err_kind, 0, 4);
+        next[s] = (int32_t)s;
+        return;
+    }
+    uint32_t src = (uint32_t)ck;
+    uint32_t dst = (uint32_t)row_keys[src];
+    if ((int64_t)dst >= n) {
+        atomicCAS(&status->err_kind, 0, 2);
+        next[s] = (int32_t)s;
+        return;
+    }
+    next[s] = label[dst];
+    esrc[s] = src;
+    edst[s] = dst;
+    ew[s] = __uint_as_float((uint32_t)(ck >> 32));
+}
+
+// ---- exclusive scan of int32 (three passes) ----
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *warp_sums, int &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < (SCAN_THREADS / 32) ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < (SCAN_THREADS / 32)) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    int warp_prefix = warp > 0 ? warp_sums[warp - 1] : 0;
+    total = warp_sums[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void scan_tiles_kernel(const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                  int64_t n, int32_t *__restrict__ tile_sums) {
+    __shared__ int warp_sums[SCAN_THREADS / 32];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int sum = 0;
+#pragma unroll
+    for (int t = 0; t < SCAN_ITEMS; ++t) {
+        v[t] = base + t < n ? in[base + t] : 0;
+        sum += v[t];
+    }
+    int total;
+    int prefix = block_exclusive_scan(sum, warp_sums, total);
+#pragma unroll
+    for (int t = 0; t < SCAN_ITEMS; ++t) {
+        if (base + t < n) out[base + t] = prefix;
+        prefix += v[t];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void scan_sums_kernel(int32_t *__restrict__ sums, int64_t tiles,
+                                 int32_t *__restrict__ grand_total) {
+    __shared__ int warp_sums[SCAN_THREADS / 32];
+    int carry = 0;
+    for (int64_t b = 0; b < tiles; b += SCAN_THREADS) {
+        int64_t i = b + threadIdx.x;
+        int v = i < tiles ? sums[i] : 0;
+        int total;
+        int p = block_exclusive_scan(v, warp_sums, total);
+        if (i < tiles) sums[i] = carry + p;
+        carry += total;
+    }
+    if (threadIdx.x == 0 && grand_total) *grand_total = carry;
+}
+
+__global__ void scan_add_kernel(int32_t *__restrict__ out, int64_t n,
+                                const int32_t *__restrict__ sums) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += sums[i / SCAN_TILE];
+}
+
+inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
+
+}  // namespace
+
+int scan_exclusive(cuscan_ctx *ctx, const int32_t *in, int32_t *out, int64_t n,
+                   int32_t *grand_total, Buffer &tmp, cudaStream_t s) {
+    const int64_t tiles = ceil_div(n > 0 ? n : 1, SCAN_TILE);
+    int rc = ensure(ctx, tmp, (size_t)tiles * sizeof(int32_t), "scan tile sums");
+    if (rc) return rc;
+    CUSCAN_KERNEL(scan_tiles_kernel, (unsigned)tiles, SCAN_THREADS, 0, s, in, out, n, as<int32_t>(tmp));
+    CUSCAN_KERNEL(scan_sums_kernel, 1, SCAN_THREADS, 0, s, as<int32_t>(tmp), tiles, grand_total);
+    CUSCAN_KERNEL(scan_add_kernel, blocks(n), 256, 0, s, out, n, as<int32_t>(tmp));
+    CUSCAN_LAUNCH(ctx, "scan_exclusive");
+    return CUSCAN_OK;
+}
+
+int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
+                float *core, cudaStream_t s) {
+    CUSCAN_KERNEL(core_kernel, blocks(n), 256, 0, s, knn_sq, n, k, min_samples, core);
+    CUSCAN_LAUNCH(ctx, "core_kernel");
+    return CUSCAN_OK;
+}
+
+static int log2_ceil(int64_t c) {
+    int l = 0;
+    while ((1ll << l) < c) ++l;
+    return l;
+}
+
+// Common tail of the seed and of every round: break cycles of the proposals next[] over the
+// active nodes, append the kept edges in node order, merge and relabel points.
+static int resolve_proposals(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t active,
+                             const int32_t *active_label, int32_t *point_label,
+                             uint32_t *out_src, uint32_t *out_dst, float *out_w,
+                             int require_progress, cudaStream_t s) {
+    int32_t *next = as<int32_t>(b.next);
+    int32_t *ja = as<int32_t>(b.jmp_a), *ma = as<int32_t>(b.mx_a);
+    int32_t *jb = as<int32_t>(b.jmp_b), *mb = as<int32_t>(b.mx_b);
+    CUSCAN_KERNEL(dbl_init_kernel, blocks(n), 256, 0, s, next, active_label, n, ja, ma);
+    const int steps = log2_ceil(active > 1 ? active : 2) + 1;
+    for (int t = 0; t < steps; ++t) {
+        CUSCAN_KERNEL(dbl_step_kernel, blocks(n), 256, 0, s, ja, ma, active_label, n, jb, mb);
+        int32_t *tj = ja, *tm = ma;
+        ja = jb;
+        ma = mb;
+        jb = tj;
+        mb = tm;
+    }
+    int32_t *keep = as<int32_t>(b.keep), *pos = as<int32_t>(b.pos), *parent = as<int32_t>(b.parent);
+    CUSCAN_KERNEL(keep_kernel, blocks(n), 256, 0, s, next, ja, ma, active_label, n, keep, parent);
+    CUSCAN_LAUNCH(ctx, "cycle breaking");
+    int rc = scan_exclusive(ctx, keep, pos, n, as<int32_t>(b.kept_total), b.scan_tmp, s);
+    if (rc) return rc;
+    CUSCAN_KERNEL(emit_kernel, blocks(n), 256, 0, s, keep, pos, as<uint32_t>(b.esrc), as<uint32_t>(b.edst),
+                                           as<float>(b.ew), n, b.status, out_src, out_dst, out_w,
+                                           n - 1);
+    CUSCAN_KERNEL(add_edges_kernel, 1, 1, 0, s, b.status, as<int32_t>(b.kept_total), require_progress);
+    for (int t = 0; t < steps; ++t) CUSCAN_KERNEL(jump_kernel, blocks(n), 256, 0, s, parent, active_label, n);
+    int32_t *minlab = as<int32_t>(b.minlab);
+    CUSCAN_KERNEL(minlab_init_kernel, blocks(n), 256, 0, s, parent, active_label, n, minlab);
+    CUSCAN_KERNEL(minlab_reduce_kernel, blocks(n), 256, 0, s, parent, active_label, n, minlab);
+    CUSCAN_KERNEL(relabel_kernel, blocks(n), 256, 0, s, point_label, parent, minlab, n);
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(&b.status->components, 0, sizeof(unsigned long long), s));
+    CUSCAN_KERNEL(count_components_kernel, blocks(n), 256, 0, s, point_label, n, b.status);
+    CUSCAN_LAUNCH(ctx, "union/relabel");
+    return CUSCAN_OK;
+}
+
+int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int32_t *ids,
+                const float *dsq, int64_t n, int k, int32_t *label, uint32_t *out_src,
+                uint32_t *out_dst, float *out_w, cudaStream_t s) {
+    CUSCAN_KERNEL(seed_kernel, blocks(n), 256, 0, s, core, ids, dsq, n, k, as<int32_t>(b.next),
+                                           as<uint32_t>(b.esrc), as<uint32_t>(b.edst),
+                                           as<float>(b.ew), b.status);
+    CUSCAN_KERNEL(iota_kernel, blocks(n), 256, 0, s, label, n);
+    CUSCAN_LAUNCH(ctx, "seed_kernel");
+    // all points are active nodes of the seed graph (active_label == nullptr)
+    int rc = resolve_proposals(ctx, b, n, n, nullptr, label, out_src, out_dst, out_w, 0, s);
+    if (rc) return rc;
+    return CUSCAN_OK;
+}
+
+int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, const float *core,
+                             const int32_t *label, int64_t n, int d, cudaStream_t s) {
+    int32_t *cnt = as<int32_t>(b.cnt), *start = as<int32_t>(b.start), *fill = as<int32_t>(b.fill);
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(fill, 0, sizeof(int32_t) * n, s));
+    CUSCAN_KERNEL(hist_kernel, blocks(n), 256, 0, s, label, n, cnt);
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(&b.status->same_pairs, 0, sizeof(double), s));
+    CUSCAN_KERNEL(same_pairs_kernel, blocks(n), 256, 0, s, cnt, n, b.status);
+    CUSCAN_LAUNCH(ctx, "hist_kernel");
+    int rc = scan_exclusive(ctx, cnt, start, n, nullptr, b.scan_tmp, s);
+    if (rc) return rc;
+    CUSCAN_KERNEL(scatter_kernel, blocks(n), 256, 0, s, label, n, start, fill, as<int32_t>(b.perm));
+    CUSCAN_KERNEL(gather_kernel, blocks(n * d), 256, 0, s, x, core, label, as<int32_t>(b.perm), n, d,
+                                                 as<float>(b.xp), as<float>(b.corep),
+                                                 as<int32_t>(b.labp));
+    CUSCAN_LAUNCH(ctx, "component sort");
+    return CUSCAN_OK;
+}
+
+int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t components,
+                 int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
+                 cudaStream_t s) {
+    unsigned long long *comp_keys = as<unsigned long long>(b.comp_keys);
+    int rc = launch_fill_u64(ctx, comp_keys, n, ~0ull, s);
+    if (rc) return rc;
+    CUSCAN_KERNEL(component_min_kernel, blocks(n), 256, 0, s, as<int32_t>(b.perm), as<int32_t>(b.labp),
+                                                   as<unsigned long long>(b.row_keys), n,
+                                                   comp_keys, b.status);
+    CUSCAN_KERNEL(winner_kernel, blocks(n), 256, 0, s, label, comp_keys, as<unsigned long long>(b.row_keys),
+                                             n, as<int32_t>(b.next), as<uint32_t>(b.esrc),
+                                             as<uint32_t>(b.edst), as<float>(b.ew), b.status);
+    CUSCAN_LAUNCH(ctx, "component winners");
+    return resolve_proposals(ctx, b, n, components, label, label, out_src, out_dst, out_w, 1, s);
+}
+
+int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d) {
+    const size_t ni = sizeof(int32_t) * (size_t)n;
+    int rc = 0;
+#define RES(buf, bytes, what) \
+    if ((rc = ensure(ctx, b.buf, (bytes), what))) return rc;
+    RES(next, ni, "forest proposals");
+    RES(esrc, ni, "forest sources");
+    RES(edst, ni, "forest destinations");
+    RES(ew, sizeof(float) * (size_t)n, "forest weights");
+    RES(jmp_a, ni, "pointer doubling");
+    RES(mx_a, ni, "pointer doubling");
+    RES(jmp_b, ni, "pointer doubling");
+    RES(mx_b, ni, "pointer doubling");
+    RES(keep, ni, "kept edges");
+    RES(pos, ni, "edge positions");
+    RES(parent, ni, "forest parents");
+    RES(minlab, ni, "component labels");
+    RES(kept_total, 64, "kept total");
+    RES(cnt, ni, "component histogram");
+    RES(start, ni, "component offsets");
+    RES(fill, ni, "component cursors");
+    RES(perm, ni, "component order");
+    RES(xp, sizeof(float) * (size_t)n * (size_t)d, "component-sorted data");
+    RES(corep, sizeof(float) * (size_t)n, "component-sorted core distances");
+    RES(labp, ni, "component-sorted labels");
+    RES(row_keys, sizeof(unsigned long long) * (size_t)n, "row candidates");
+    RES(comp_keys, sizeof(unsigned long long) * (size_t)n, "component candidates");
+    RES(tile_lo, sizeof(int32_t) * (size_t)(ceil_div(n, 32) + 1), "tile label ranges");
+    RES(tile_hi, sizeof(int32_t) * (size_t)(ceil_div(n, 32) + 1), "tile label ranges");
+    RES(status_buf, sizeof(DevStatus), "fit status");
+#undef RES
+    b.status = as<DevStatus>(b.status_buf);
+    return CUSCAN_OK;
+}
+
+void forest_release(ForestBuffers &b) {
+    Buffer *all[] = {&b.next, &b.esrc, &b.edst, &b.ew, &b.jmp_a, &b.mx_a, &b.jmp_b, &b.mx_b,
+                     &b.keep, &b.pos, &b.parent, &b.minlab, &b.kept_total, &b.cnt, &b.start,
+                     &b.fill, &b.perm, &b.xp, &b.corep, &b.labp, &b.row_keys, &b.comp_keys,
+                     &b.tile_lo, &b.tile_hi, &b.status_buf, &b.scan_tmp, &b.knn_ids_tmp,
+                     &b.knn_dist_tmp};
+    for (Buffer *p : all) release(*p);
+    b.status = nullptr;
+}
+
+}  // namespace cuscan

@@ -1,0 +1,49 @@
+// Device buffers and entry points of the MST integer work (forest.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace cuscan {
+
+// Small status block that the host reads once per Borůvka round.
+struct DevStatus {
+    unsigned long long components;  // components after the last merge
+    unsigned long long edges;       // MST edges emitted so far
+    double same_pairs;     // sum of squared component sizes entering the current round
+    int err_kind;          // 0 ok, 1 numerical weight, 2 index out of range, 4 no progress
+    int pad[3];
+};
+
+struct ForestBuffers {
+    Buffer next, esrc, edst, ew;            // proposals per node
+    Buffer jmp_a, mx_a, jmp_b, mx_b;        // pointer doubling
+    Buffer keep, pos, parent, minlab, kept_total;
+    Buffer cnt, start, fill, perm;          // counting sort by component
+    Buffer xp, corep, labp;                 // component-sorted copies
+    Buffer row_keys, comp_keys;             // 64-bit candidate keys
+    Buffer tile_lo, tile_hi;                // label range per 32-row tile
+    Buffer status_buf, scan_tmp;
+    Buffer knn_ids_tmp, knn_dist_tmp;       // split-kNN partial lists
+    DevStatus *status = nullptr;
+};
+
+int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
+void forest_release(ForestBuffers &b);
+int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
+                float *core, cudaStream_t s);
+// Seed forest (mst.rs:368-420): appends the kept seed edges and labels points by the smallest
+// point of their tree; status->components is refreshed.
+int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int32_t *ids,
+                const float *dsq, int64_t n, int k, int32_t *label, uint32_t *out_src,
+                uint32_t *out_dst, float *out_w, cudaStream_t s);
+// Group points by label: perm, xp, corep, labp.
+int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, const float *core,
+                             const int32_t *label, int64_t n, int d, cudaStream_t s);
+// Merge one round from the per-row candidate keys in b.row_keys.
+int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t components,
+                 int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
+                 cudaStream_t s);
+int scan_exclusive(cuscan_ctx *ctx, const int32_t *in, int32_t *out, int64_t n,
+                   int32_t *grand_total, Buffer &tmp, cudaStream_t s);
+
+}  // namespace cuscan

@@ -1,0 +1,354 @@
+// Exact k-nearest-neighbour sweep with f32 direct differences (the "plain" arithmetic).
+//
+// Semantics follow exact_kernel (crates/cuscan-common/src/kernels/neighbors.rs:17-76): every
+// squared distance is acc = fmaf(q_f - r_f, q_f - r_f, acc) over features in order, rows are
+// ordered by (distance, id), self is excluded by global id, empty slots hold (pad, nr).
+//
+// Layout: one thread owns one query row (its features staged once in shared memory as
+// [feature][query] so the per-feature reads are conflict free); reference rows stream through
+// a double-buffered shared tile [feature][RT] filled with 4-byte cp.async copies, and each
+// thread keeps RT running distances in registers. Per feature and per 4 references that is one
+// broadcast 16-byte shared load, four FADD and four FFMA. The running top-K list lives in
+// registers and is updated with a fully unrolled predicated insertion; after the first few
+// tiles almost every candidate fails the threshold test, so the list costs one compare per
+// pair. When there are too few query blocks to fill the 152 SMs the reference range is split
+// across blocks and the partial lists are merged by a second kernel.
+#include <limits>
+
+#include "common.cuh"
+
+namespace cuscan {
+namespace {
+
+constexpr int QB = 128;  // queries (threads) per block
+constexpr int RT = 32;   // references per shared tile
+constexpr int RTP = 36;  // padded tile row (keeps 16-byte alignment, spreads store banks)
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem, bool valid) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    int src_size = valid ? 4 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem),
+                 "r"(src_size));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Copy reference rows [r0, r0+RT) into tile[f*RTP + r] (zero fill past nr).
+__device__ __forceinline__ void load_ref_tile(float *tile, const float *ref, int64_t nr, int d,
+                                              int64_t r0) {
+    const int total = RT * d;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        int r = e / d;
+        int f = e - r * d;
+        int64_t row = r0 + r;
+        bool valid = row < nr;
+        const float *src = valid ? ref + row * (int64_t)d + f : ref;
+        cp_async4(&tile[f * RTP + r], src, valid);
+    }
+}
+
+// Sorted register list insertion: (x, j) is known to beat slot K-1.
+template <int K>
+__device__ __forceinline__ void list_insert(float (&ld)[K], int (&li)[K], float x, int j) {
+#pragma unroll
+    for (int s = K - 1; s >= 0; --s) {
+        bool here = knn_better(x, j, ld[s], li[s]);
+        bool prev = (s > 0) ? knn_better(x, j, ld[s > 0 ? s - 1 : 0], li[s > 0 ? s - 1 : 0]) : false;
+        if (here) {
+            if (prev) {
+                ld[s] = ld[s - 1 < 0 ? 0 : s - 1];
+                li[s] = li[s - 1 < 0 ? 0 : s - 1];
+            } else {
+                ld[s] = x;
+                li[s] = j;
+            }
+        }
+    }
+}
+
+// One block: QB query rows x reference rows [r_begin, r_end). Writes the K-best list of each
+// query (first k entries) to out_ids/out_dist rows of width k (partial lists when split).
+template <int K>
+__global__ void __launch_bounds__(QB) knn_fp32_kernel(
+    const float *__restrict__ query, int64_t nq, const float *__restrict__ ref, int64_t nr, int d,
+    int k, int exclude_self, int64_t query_offset, float pad, int64_t ref_chunk,
+    int32_t *__restrict__ out_ids, float *__restrict__ out_dist, int64_t out_split_stride) {
+    extern __shared__ __align__(16) float smem[];
+    float *qs = smem;                         // [d][QB]
+    float *tiles = smem + (size_t)d * QB;     // 2 x [d][RTP]
+    const int tid = threadIdx.x;
+    const int64_t q0 = (int64_t)blockIdx.x * QB;
+    const int64_t qi = q0 + tid;
+    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
+    int64_t r_end = r_begin + ref_chunk;
+    if (r_end > nr) r_end = nr;
+
+    // stage this block's queries transposed
+    for (int e = tid; e < QB * d; e += QB) {
+        int q = e / d;
+        int f = e - q * d;
+        int64_t row = q0 + q;
+        qs[f * QB + q] = row < nq ? query[row * (int64_t)d + f] : 0.0f;
+    }
+
+    float ld[K];
+    int li[K];
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+        ld[s] = pad;
+        li[s] = (int)nr;
+    }
+    const int64_t self = exclude_self ? query_offset + qi : -1;
+
+    const int tile_floats = d * RTP;
+    int buf = 0;
+    if (r_begin < r_end) {
+        load_ref_tile(tiles, ref, r_end, d, r_begin);
+        cp_async_commit();
+    }
+    for (int64_t r0 = r_begin; r0 < r_end; r0 += RT) {
+        const int64_t next = r0 + RT;
+        if (next < r_end) {
+            load_ref_tile(tiles + (buf ^ 1) * tile_floats, ref, r_end, d, next);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const float *tile = tiles + buf * tile_floats;
+        float acc[RT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) acc[r] = 0.0f;
+        const float *qcol = qs + tid;
+#pragma unroll 2
+        for (int f = 0; f < d; ++f) {
+            const float qv = qcol[f * QB];
+            const float4 *row4 = reinterpret_cast<const float4 *>(tile + f * RTP);
+#pragma unroll
+            for (int r4 = 0; r4 < RT / 4; ++r4) {
+                const float4 v = row4[r4];
+                float t0 = qv - v.x, t1 = qv - v.y, t2 = qv - v.z, t3 = qv - v.w;
+                acc[4 * r4 + 0] = __fmaf_rn(t0, t0, acc[4 * r4 + 0]);
+                acc[4 * r4 + 1] = __fmaf_rn(t1, t1, acc[4 * r4 + 1]);
+                acc[4 * r4 + 2] = __fmaf_rn(t2, t2, acc[4 * r4 + 2]);
+                acc[4 * r4 + 3] = __fmaf_rn(t3, t3, acc[4 * r4 + 3]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RT; ++r) {
+            const int64_t j = r0 + r;
+            const float x = acc[r];
+            if (j < r_end && j != self && knn_better(x, (int)j, ld[K - 1], li[K - 1]))
+                list_insert<K>(ld, li, x, (int)j);
+        }
+        __syncthreads();
+        buf ^= 1;
+    }
+    if (qi < nq) {
+        int32_t *oi = out_ids + (int64_t)blockIdx.y * out_split_stride + qi * k;
+        float *od = out_dist + (int64_t)blockIdx.y * out_split_stride + qi * k;
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            if (s < k) {
+                oi[s] = li[s];
+                od[s] = ld[s];
+            }
+        }
+    }
+}
+
+// Merge `splits` sorted partial lists per query into the final top-k.
+template <int K>
+__global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
+                                 const float *__restrict__ part_dist, int64_t nq, int k,
+                                 int splits, int64_t split_stride, float pad, int64_t nr,
+                                 int squared, int32_t *__restrict__ ids, float *__restrict__ dist) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    float ld[K];
+    int li[K];
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+        ld[s] = pad;
+        li[s] = (int)nr;
+    }
+    for (int sp = 0; sp < splits; ++sp) {
+        const int32_t *pi = part_ids + sp * split_stride + q * k;
+        const float *pd = part_dist + sp * split_stride + q * k;
+        for (int s = 0; s < k; ++s) {
+            float x = pd[s];
+            int j = pi[s];
+            if (knn_better(x, j, ld[K - 1], li[K - 1])) list_insert<K>(ld, li, x, j);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+        if (s < k) {
+            ids[q * k + s] = li[s];
+            float x = ld[s];
+            dist[q * k + s] = squared ? x : sqrtf(x);
+        }
+    }
+}
+
+__global__ void sqrt_rows_kernel(float *dist, int64_t count) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dist[i] = sqrtf(dist[i]);
+}
+
+// General k: one thread per query keeps its list in the output row in global memory,
+// exactly like the reference's serial kernel (used for k > 32).
+__global__ void __launch_bounds__(QB) knn_fp32_wide_kernel(
+    const float *__restrict__ query, int64_t nq, const float *__restrict__ ref, int64_t nr, int d,
+    int k, int exclude_self, int64_t query_offset, float pad, int32_t *__restrict__ ids,
+    float *__restrict__ dist) {
+    extern __shared__ __align__(16) float smem[];
+    float *qs = smem;
+    float *tile = smem + (size_t)d * QB;
+    const int tid = threadIdx.x;
+    const int64_t q0 = (int64_t)blockIdx.x * QB;
+    const int64_t qi = q0 + tid;
+    for (int e = tid; e < QB * d; e += QB) {
+        int q = e / d;
+        int f = e - q * d;
+        int64_t row = q0 + q;
+        qs[f * QB + q] = row < nq ? query[row * (int64_t)d + f] : 0.0f;
+    }
+    int32_t *li = ids + (qi < nq ? qi : 0) * (int64_t)k;
+    float *ld = dist + (qi < nq ? qi : 0) * (int64_t)k;
+    if (qi < nq)
+        for (int s = 0; s < k; ++s) {
+            li[s] = (int32_t)nr;
+            ld[s] = pad;
+        }
+    float worst_d = pad;
+    int worst_i = (int)nr;
+    const int64_t self = exclude_self ? query_offset + qi : -1;
+    for (int64_t r0 = 0; r0 < nr; r0 += RT) {
+        __syncthreads();
+        load_ref_tile(tile, ref, nr, d, r0);
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncthreads();
+        float acc[RT];
+#pragma unroll
+        for (int r = 0; r < RT; ++r) acc[r] = 0.0f;
+        for (int f = 0; f < d; ++f) {
+            const float qv = qs[f * QB + tid];
+            const float4 *row4 = reinterpret_cast<const float4 *>(tile + f * RTP);
+#pragma unroll
+            for (int r4 = 0; r4 < RT / 4; ++r4) {
+                const float4 v = row4[r4];
+                float t0 = qv - v.x, t1 = qv - v.y, t2 = qv - v.z, t3 = qv - v.w;
+                acc[4 * r4 + 0] = __fmaf_rn(t0, t0, acc[4 * r4 + 0]);
+                acc[4 * r4 + 1] = __fmaf_rn(t1, t1, acc[4 * r4 + 1]);
+                acc[4 * r4 + 2] = __fmaf_rn(t2, t2, acc[4 * r4 + 2]);
+                acc[4 * r4 + 3] = __fmaf_rn(t3, t3, acc[4 * r4 + 3]);
+            }
+        }
+        if (qi < nq) {
+            for (int r = 0; r < RT; ++r) {
+                const int64_t j = r0 + r;
+                const float x = acc[r];
+                if (j >= nr || j == self || !knn_better(x, (int)j, worst_d, worst_i)) continue;
+                int slot = k - 1;
+                while (slot > 0 && knn_better(x, (int)j, ld[slot - 1], li[slot - 1])) {
+                    li[slot] = li[slot - 1];
+                    ld[slot] = ld[slot - 1];
+                    --slot;
+                }
+                li[slot] = (int32_t)j;
+                ld[slot] = x;
+                worst_d = ld[k - 1];
+                worst_i = li[k - 1];
+            }
+        }
+    }
+}
+
+template <int K>
+int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, int64_t nr, int d,
+            int k, int exclude_self, int64_t query_offset, int squared, int32_t *ids, float *dist,
+            cudaStream_t s, Buffer &scratch_ids, Buffer &scratch_dist) {
+    const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
+    const int64_t qblocks = ceil_div(nq, QB);
+    // Split the reference range when the query blocks alone cannot fill the GPU.
+    int64_t splits = 1;
+    const int64_t target = 2 * (int64_t)ctx->sm_count;
+    if (qblocks < target) splits = ceil_div(target, qblocks);
+    const int64_t max_splits = ceil_div(nr, (int64_t)RT * 8);
+    if (splits > max_splits) splits = max_splits;
+    if (splits > 64) splits = 64;
+    if (splits < 1) splits = 1;
+    int64_t chunk = ceil_div(ceil_div(nr, splits), RT) * RT;
+    splits = ceil_div(nr, chunk);
+    const size_t smem = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
+    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(knn_fp32_kernel<K>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)qblocks, (unsigned)splits);
+    if (splits == 1) {
+        CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k, exclude_self,
+                                                   query_offset, pad, chunk, ids, dist, 0);
+        CUSCAN_LAUNCH(ctx, "knn_fp32_kernel");
+        if (!squared && nq * k > 0) {
+            CUSCAN_KERNEL(sqrt_rows_kernel, (unsigned)ceil_div(nq * k, 256), 256, 0, s, dist, nq * k);
+            CUSCAN_LAUNCH(ctx, "sqrt_rows_kernel");
+        }
+        return CUSCAN_OK;
+    }
+    const int64_t stride = nq * k;
+    int rc = ensure(ctx, scratch_ids, (size_t)(stride * splits) * sizeof(int32_t), "kNN partial ids");
+    if (rc) return rc;
+    rc = ensure(ctx, scratch_dist, (size_t)(stride * splits) * sizeof(float), "kNN partial distances");
+    if (rc) return rc;
+    CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k, exclude_self, query_offset,
+                                               pad, chunk, as<int32_t>(scratch_ids),
+                                               as<float>(scratch_dist), stride);
+    CUSCAN_LAUNCH(ctx, "knn_fp32_kernel");
+    CUSCAN_KERNEL(knn_merge_kernel<K>, (unsigned)ceil_div(nq, 128), 128, 0, s, 
+        as<int32_t>(scratch_ids), as<float>(scratch_dist), nq, k, (int)splits, stride, pad, nr,
+        squared, ids, dist);
+    CUSCAN_LAUNCH(ctx, "knn_merge_kernel");
+    return CUSCAN_OK;
+}
+
+}  // namespace
+
+int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref,
+                          int64_t nr, int d, int k, int exclude_self, int64_t query_offset,
+                          int squared, int32_t *ids, float *dist, cudaStream_t s,
+                          Buffer &scratch_ids, Buffer &scratch_dist) {
+    if (nq == 0) return CUSCAN_OK;
+    const size_t smem_needed = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
+    if (smem_needed > 200 * 1024)
+        return fail(ctx, CUSCAN_CAPACITY,
+                    "feature count %d exceeds the shared-memory staging limit of the kNN kernel "
+                    "(at most 320 features)", d);
+    if (k <= 8)
+        return run_knn<8>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared, ids,
+                          dist, s, scratch_ids, scratch_dist);
+    if (k <= 16)
+        return run_knn<16>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared,
+                           ids, dist, s, scratch_ids, scratch_dist);
+    if (k <= 32)
+        return run_knn<32>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared,
+                           ids, dist, s, scratch_ids, scratch_dist);
+    const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
+    const size_t smem = ((size_t)d * QB + (size_t)d * RTP) * sizeof(float);
+    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(knn_fp32_wide_kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUSCAN_KERNEL(knn_fp32_wide_kernel, (unsigned)ceil_div(nq, QB), QB, smem, s,
+        query, nq, ref, nr, d, k, exclude_self, query_offset, pad, ids, dist);
+    CUSCAN_LAUNCH(ctx, "knn_fp32_wide_kernel");
+    if (!squared) {
+        CUSCAN_KERNEL(sqrt_rows_kernel, (unsigned)ceil_div(nq * k, 256), 256, 0, s, dist, nq * k);
+        CUSCAN_LAUNCH(ctx, "sqrt_rows_kernel");
+    }
+    return CUSCAN_OK;
+}
+
+}  // namespace cuscan

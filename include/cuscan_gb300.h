@@ -1,0 +1,204 @@
+/*
+ * cuscan_gb300: GB300-native (sm_103a) HDBSCAN fit core behind a plain C ABI.
+ *
+ * The entry points replace, one for one, the device operations that lega0208/cuscan routes
+ * through its Burn/CubeCL backend extension for the exact complete-graph HDBSCAN fit:
+ *
+ *   cuscan_exact_knn            <- NeighborOps::exact_neighbors
+ *                                  (crates/cuscan-common/src/backend.rs:13-20,
+ *                                   crates/cuscan-common/src/neighbors.rs:148-165)
+ *   cuscan_boruvka_candidates   <- HdbscanOps::boruvka_candidates
+ *                                  (crates/hdbscan/src/backend.rs:75-81)
+ *   cuscan_component_reduce     <- HdbscanOps::component_reduce
+ *                                  (crates/hdbscan/src/backend.rs:90-98)
+ *   cuscan_fit_core[_device]    <- core_distances + spanning_tree of the brute-force
+ *                                  complete-graph route, fused and device resident
+ *                                  (crates/hdbscan/src/estimator.rs:524-874)
+ *   cuscan_clusters_from_spanning_tree
+ *                               <- hdbscan_core::clusters_from_spanning_tree
+ *                                  (crates/hdbscan-core/src/lib.rs:57-97), host code
+ *
+ * Conventions
+ *  - Every function returns a cuscan_status (0 = success). The message of the last failure
+ *    on a context is read with cuscan_last_error(); the status values map one to one onto the
+ *    reference's HdbscanError variants (crates/hdbscan-core/src/error.rs:8-19).
+ *  - Pointers are caller owned. "device" arguments are CUDA device pointers on the context's
+ *    device; "host" arguments are ordinary host memory. No function keeps a pointer after it
+ *    returns.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the context's own stream. Device
+ *    entry points only enqueue work on that stream, except where a function states it
+ *    synchronises.
+ *  - Row-major float32 data, int32 ids, n < 2^31 rows.
+ */
+#ifndef CUSCAN_GB300_H
+#define CUSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cuscan_status {
+    CUSCAN_OK = 0,
+    CUSCAN_INVALID_CONFIG = 1,      /* HdbscanError::InvalidConfig */
+    CUSCAN_INVALID_INPUT = 2,       /* HdbscanError::InvalidInput */
+    CUSCAN_BACKEND_UNAVAILABLE = 3, /* HdbscanError::BackendUnavailable (no device, CUDA error) */
+    CUSCAN_NUMERICAL = 4,           /* HdbscanError::Numerical */
+    CUSCAN_OVERFLOW = 5,            /* HdbscanError::Overflow */
+    CUSCAN_CAPACITY = 6,            /* HdbscanError::Capacity */
+    CUSCAN_MEMORY = 7               /* HdbscanError::Memory */
+} cuscan_status;
+
+/* Arithmetic used by the distance sweeps of cuscan_fit_core. Both give bit-identical results:
+ * PLAIN evaluates every pair with exact f32 direct differences on the SIMT cores;
+ * BF16_REFINED screens pairs with bf16 tensor-core GEMM tiles and re-evaluates every pair that
+ * the proven error bound cannot rule out with the same exact f32 direct differences. */
+typedef enum cuscan_precision {
+    CUSCAN_PRECISION_PLAIN = 0,
+    CUSCAN_PRECISION_BF16_REFINED = 1
+} cuscan_precision;
+
+typedef struct cuscan_ctx cuscan_ctx;
+
+/* Per-fit counters and stage times (milliseconds, CUDA events on the fit stream). */
+typedef struct cuscan_fit_stats {
+    double core_ms;          /* kNN sweep + core distances ("core_distances" stage) */
+    double mst_ms;           /* seed + all Boruvka rounds ("mst" stage) */
+    double knn_kernel_ms;    /* the kNN distance-sweep kernels alone */
+    double candidate_kernel_ms; /* the Boruvka candidate kernels alone, summed over rounds */
+    int64_t rounds;          /* Boruvka rounds after the kNN seed */
+    int64_t seed_edges;      /* edges added by the kNN seed */
+    int64_t components_after_seed;
+    int64_t refined_rows;    /* rows re-evaluated exactly after the bf16 screen */
+    int64_t fallback_rows;   /* rows whose bf16 screen was inconclusive and ran exact */
+    double cross_pairs;      /* sum over rounds of ordered cross-component pairs */
+} cuscan_fit_stats;
+
+/* ---- context ---- */
+int cuscan_ctx_create(int device, cuscan_ctx **out);
+void cuscan_ctx_destroy(cuscan_ctx *ctx);
+const char *cuscan_last_error(const cuscan_ctx *ctx);
+int cuscan_error_kind(const cuscan_ctx *ctx);
+/* The context's own CUDA stream (cudaStream_t as void*). */
+void *cuscan_ctx_stream(cuscan_ctx *ctx);
+/* Library version string. */
+const char *cuscan_version(void);
+/* Number of CUDA kernels this library has launched in the process so far (all contexts). */
+int64_t cuscan_launch_count(void);
+
+/*
+ * Exact k nearest neighbours of `query` rows among `reference` rows (all device pointers),
+ * ordered by (squared distance, reference id). With exclude_self, reference row
+ * query_offset + i is skipped for query row i. Missing neighbours are padded with id nr and
+ * distance +inf (squared) or sqrt(FLT_MAX) (unsquared); unsquared output is the sqrt of the
+ * squared value. Replaces NeighborOps::exact_neighbors
+ * (crates/cuscan-common/src/kernels/neighbors.rs:17-76 semantics).
+ */
+int cuscan_exact_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *reference,
+                     int64_t nr, int32_t d, int32_t k, int32_t exclude_self,
+                     int64_t query_offset, int32_t squared, int32_t *ids_out, float *dist_out,
+                     void *stream);
+
+/*
+ * Per-row Borůvka candidate: for every row i the lexicographically smallest
+ * (max(max(d2_ij, core_sq_i), core_sq_j), j) over rows j with components[j] != components[i];
+ * rows without a candidate get (+inf, n). Device pointers. Replaces
+ * HdbscanOps::boruvka_candidates (crates/hdbscan/src/backend.rs:75-81;
+ * crates/hdbscan/src/kernels/boruvka.rs:68-140).
+ */
+int cuscan_boruvka_candidates(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                              const int32_t *components, int64_t n, int32_t d, float *weights_out,
+                              int32_t *destinations_out, void *stream);
+
+/*
+ * Per-component winner over a stable CSR component plan (device pointers). weights/indices
+ * are the per-row candidates; members/tile_starts/tile_ends/partial_offsets are the
+ * ComponentReductionPlan arrays (crates/hdbscan-core/src/mst.rs:30-147). Outputs:
+ * win_weights[c] (original weight bits of the winner, +inf when absent) and
+ * win_meta[c*5] = (source, destination, bad_row, error_kind, bad_destination), exactly as
+ * HdbscanOps::component_reduce (crates/hdbscan/src/backend.rs:90-98;
+ * crates/hdbscan/src/kernels/component_reduce.rs:28-353).
+ */
+int cuscan_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t *indices,
+                            const int32_t *members, const int32_t *tile_starts,
+                            const int32_t *tile_ends, const int32_t *partial_offsets, int64_t n,
+                            int64_t p, int64_t c, float *win_weights, int32_t *win_meta,
+                            void *stream);
+
+/*
+ * Fused exact fit core of the brute-force complete-graph route: kNN core distances
+ * (k = min(min_samples, n-1)), kNN seed forest, then Borůvka rounds until one component
+ * remains, all on the device. Inputs and outputs are HOST pointers; the function copies the
+ * data in, runs the fit on the context stream and synchronises before returning.
+ * Outputs: knn_ids[n*k], knn_sq[n*k] (may be NULL), core_sq[n], and the n-1 MST edges
+ * (src, dst, squared weight) in the reference's merge order: seed edges by point, then each
+ * round's winners by component first appearance (crates/hdbscan/src/estimator.rs:689-874).
+ * Callers finalise with sqrt((double) w) and sort by (weight, src, dst)
+ * (crates/hdbscan-core/src/mst.rs:501-512). stats may be NULL.
+ */
+int cuscan_fit_core(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                    int32_t min_samples, int32_t precision, int32_t *knn_ids, float *knn_sq,
+                    float *core_sq, uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                    int64_t *n_edges, cuscan_fit_stats *stats);
+
+/*
+ * Same as cuscan_fit_core with every array a DEVICE pointer (data resident in HBM). The call
+ * enqueues on `stream`, synchronises it once per Borůvka round to read the component count,
+ * and returns when the fit is complete.
+ */
+int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                           int32_t min_samples, int32_t precision, int32_t *knn_ids,
+                           float *knn_sq, float *core_sq, uint32_t *mst_src, uint32_t *mst_dst,
+                           float *mst_wsq, int64_t *n_edges, cuscan_fit_stats *stats,
+                           void *stream);
+
+/* ---- host-side extraction (no device work) ---- */
+
+typedef struct cuscan_extract_config {
+    int64_t min_cluster_size;
+    int32_t selection_leaf;        /* 0 = excess of mass, 1 = leaf */
+    int32_t allow_single_cluster;
+    int64_t max_cluster_size;      /* <= 0 means unbounded */
+    double cluster_selection_epsilon;
+    double cluster_selection_persistence;
+} cuscan_extract_config;
+
+typedef struct cuscan_clustering cuscan_clustering;
+
+/*
+ * Run sort_mst, mst_to_linkage, condense_tree, simplify_hierarchy, select_clusters,
+ * labels and membership strengths on an MST of m = n_points - 1 edges (host pointers:
+ * src[m], dst[m], weight[m] Euclidean f64). Mirrors hdbscan_core::clusters_from_spanning_tree
+ * (crates/hdbscan-core/src/lib.rs:57-97). The result is read with the accessors below and
+ * freed with cuscan_clustering_free.
+ */
+int cuscan_clusters_from_spanning_tree(const uint32_t *src, const uint32_t *dst,
+                                       const double *weight, int64_t m,
+                                       const cuscan_extract_config *config,
+                                       cuscan_clustering **out, char *err, size_t err_len);
+int64_t cuscan_clustering_points(const cuscan_clustering *r);
+int64_t cuscan_clustering_condensed_rows(const cuscan_clustering *r);
+/* labels[n], probabilities[n], linkage[m*4] (left, right, distance, size),
+ * sorted_mst[m*3] (src, dst, weight), condensed parent/child/lambda/child_size[rows]. */
+void cuscan_clustering_read(const cuscan_clustering *r, int32_t *labels, float *probabilities,
+                            double *linkage, double *sorted_mst, int64_t *condensed_parent,
+                            int64_t *condensed_child, float *condensed_lambda,
+                            float *condensed_child_size);
+void cuscan_clustering_free(cuscan_clustering *r);
+
+/*
+ * DBSCAN labels at a strict single-linkage distance cut: rows of `linkage` ([rows*4] as
+ * above) with distance < cut are merged, groups smaller than min_size are noise (-1), the
+ * rest are numbered by their representative. labels_out has rows+1 entries. Mirrors
+ * hdbscan_core::labels::dbscan_cut (crates/hdbscan-core/src/labels.rs:154-209).
+ */
+int cuscan_dbscan_cut(const double *linkage, int64_t rows, double cut, int64_t min_size,
+                      int32_t *labels_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUSCAN_GB300_H */

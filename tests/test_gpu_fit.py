@@ -1,0 +1,169 @@
+"""Parity of the fused device fit core (kNN core distances + seeded Borůvka MST) with the CPU
+oracle, through the C ABI, and of the estimator's labels with the reference fixtures.
+
+Small and medium cases compare every output bit for bit, including the MST edge order (the
+reference's merge order). The full-size case checks size-independent properties instead.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cuscan_gb300 as cg
+from cuscan_gb300 import _lib, synthetic
+from oracle import oracle as O
+from tests.conftest import load_case
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = [_lib.PRECISION_PLAIN]
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def assert_fit_equal(got, exp):
+    np.testing.assert_array_equal(got["knn_ids"], exp.knn_ids)
+    np.testing.assert_array_equal(bits(got["knn_sq"]), bits(exp.knn_sq))
+    np.testing.assert_array_equal(bits(got["core_sq"]), bits(exp.core_sq))
+    np.testing.assert_array_equal(got["src"], exp.src)
+    np.testing.assert_array_equal(got["dst"], exp.dst)
+    np.testing.assert_array_equal(bits(got["wsq"]), bits(exp.wsq))
+    assert got["stats"]["rounds"] == exp.rounds
+    assert got["stats"]["seed_edges"] == exp.seed_edges
+
+
+CASES = ["blobs_d2", "blobs_d10", "blobs_d50", "moons_leaf", "varying_density",
+         "single_cluster", "duplicates_ties", "mixed_nonfinite", "overflow_finite",
+         "persistence_equal", "selection_interactions", "all_noise", "two_finite", "padding",
+         "n_below_min_samples"]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("cid", CASES)
+def test_fit_core_matches_oracle_on_fixtures(gpu_ctx, manifest, cid, precision):
+    p = {c["id"]: c for c in manifest["cases"]}[cid]["params"]
+    x = load_case(cid)["input"]
+    x = np.ascontiguousarray(x[np.isfinite(x).all(axis=1)])
+    got = gpu_ctx.fit_core(x, p["min_samples"], precision)
+    assert_fit_equal(got, O.fit_core(x, p["min_samples"]))
+
+
+def random_sets():
+    rng = np.random.default_rng(7)
+    yield "gauss", rng.normal(size=(500, 8)).astype(np.float32), 5
+    yield "lattice_ties", rng.integers(0, 5, size=(800, 3)).astype(np.float32), 4
+    base = rng.normal(size=(200, 6)).astype(np.float32)
+    yield "duplicates", np.concatenate([base, base, base[:50]]), 3
+    yield "ms1", rng.normal(size=(300, 4)).astype(np.float32), 1
+    yield "ms_ge_n", rng.normal(size=(20, 4)).astype(np.float32), 25
+    yield "line", np.arange(1000, dtype=np.float32)[:, None], 2
+    yield "blobs_5k", synthetic.blobs_with_noise(n=5000, d=16, centers=12, seed=3), 10
+    yield "aniso_8k", synthetic.anisotropic_mixture(n=8000, d=64, components=20, seed=4), 10
+    yield "vmf_6k", synthetic.vmf_like(n=6000, d=128, clusters=30, seed=5), 15
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name,x,ms", list(random_sets()), ids=lambda v: v if isinstance(v, str) else "")
+def test_fit_core_matches_oracle_on_random_sets(gpu_ctx, name, x, ms, precision):
+    got = gpu_ctx.fit_core(x, ms, precision)
+    assert_fit_equal(got, O.fit_core(x, ms))
+
+
+def test_fit_core_repeatable_and_buffers_reused(gpu_ctx):
+    x = synthetic.blobs_with_noise(n=3000, d=10, seed=9)
+    a = gpu_ctx.fit_core(x, 5)
+    small = gpu_ctx.fit_core(x[:100], 5)
+    b = gpu_ctx.fit_core(x, 5)
+    for key in ("knn_ids", "src", "dst"):
+        np.testing.assert_array_equal(a[key], b[key])
+    np.testing.assert_array_equal(bits(a["wsq"]), bits(b["wsq"]))
+    assert small["src"].shape[0] == 99
+
+
+def test_c1_workload_labels_equal_oracle_labels():
+    """blobs_2k_d10 (n=2000, d=10, 8 blobs + 5% noise, min_samples=5, mcs=5): labels, MST
+    and core distances of the estimator equal those derived from the oracle's MST."""
+    x, ms, mcs = synthetic.workload("blobs_2k_d10")
+    model = cg.HDBSCAN(min_cluster_size=mcs, min_samples=ms).fit(x)
+    fc = O.fit_core(x, ms)
+    mst = O.finalize_mst(fc.src, fc.dst, fc.wsq)
+    np.testing.assert_array_equal(model.minimum_spanning_tree_, mst)
+    host = cg.clusters_from_spanning_tree(mst[:, 0].astype(np.uint32), mst[:, 1].astype(np.uint32),
+                                          mst[:, 2], min_cluster_size=mcs)
+    np.testing.assert_array_equal(model.labels_, host["labels"])
+    np.testing.assert_array_equal(model.core_distances_, np.sqrt(fc.core_sq))
+    assert len(set(model.labels_.tolist()) - {-1}) >= 2
+
+
+@pytest.mark.parametrize("cid", ["blobs_d2", "blobs_d10", "blobs_d50", "moons_leaf",
+                                 "varying_density", "single_cluster", "mixed_nonfinite",
+                                 "overflow_finite", "persistence_equal",
+                                 "selection_interactions"])
+def test_estimator_matches_fixture_labels(manifest, cid):
+    p = {c["id"]: c for c in manifest["cases"]}[cid]["params"]
+    case = load_case(cid)
+    model = cg.HDBSCAN(min_cluster_size=p["min_cluster_size"], min_samples=p["min_samples"],
+                       cluster_selection_method=p["selection"],
+                       allow_single_cluster=p["allow_single_cluster"],
+                       max_cluster_size=p["max_cluster_size"],
+                       cluster_selection_epsilon=float(p["epsilon"]),
+                       cluster_selection_persistence=float(p["persistence"])).fit(case["input"])
+    np.testing.assert_array_equal(model.labels_, case["labels"])
+    assert np.all(np.abs(model.probabilities_ - case["probabilities"]) <= 1e-5)
+    np.testing.assert_array_equal(model.minimum_spanning_tree_[:, :2], case["mst"][:, :2])
+    np.testing.assert_array_equal(model.finite_index_, case["finite_index"])
+
+
+def test_one_finite_row_contract():
+    x = np.array([[np.nan, 1.0], [0.5, 0.5], [np.inf, 0.0]], np.float32)
+    model = cg.HDBSCAN(min_cluster_size=2).fit(x)
+    assert model.labels_.tolist() == [-1, -1, -1]
+    assert model.finite_index_.tolist() == [1]
+
+
+def check_tree_properties(x, out, ms):
+    """Size-independent checks: n-1 edges forming a spanning tree, every edge weight the exact
+    mutual reachability of its endpoints, core = kNN column, sampled kNN rows exact."""
+    n = x.shape[0]
+    src, dst, w = out["src"], out["dst"], out["wsq"]
+    assert src.shape[0] == n - 1
+    parent = np.arange(n)
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for a, b in zip(src.tolist(), dst.tolist()):
+        ra, rb = find(a), find(b)
+        assert ra != rb, "cycle"
+        parent[ra] = rb
+    d2 = O.pair_distances(x[src], x[dst])
+    core = out["core_sq"]
+    mrd = np.maximum(np.maximum(d2, core[src]), core[dst])
+    np.testing.assert_array_equal(bits(w), bits(mrd))
+    k = out["knn_ids"].shape[1]
+    if ms < n:
+        np.testing.assert_array_equal(bits(core), bits(out["knn_sq"][:, ms - 1]))
+    rng = np.random.default_rng(0)
+    rows = rng.choice(n, size=min(n, 256), replace=False)
+    for r in rows[:64]:
+        ids, ds = O.exact_neighbors(x[r:r + 1], x, k, exclude_self=True, query_offset=int(r))
+        np.testing.assert_array_equal(out["knn_ids"][r], ids[0])
+        np.testing.assert_array_equal(bits(out["knn_sq"][r]), bits(ds[0]))
+
+
+def test_full_size_fp32_workload_properties(gpu_ctx):
+    """aniso_100k_d64 (n=100000, d=64, min_samples=10) at full size."""
+    x, ms, _ = synthetic.workload("aniso_100k_d64")
+    out = gpu_ctx.fit_core(x, ms)
+    check_tree_properties(x, out, ms)
+
+
+def test_medium_workload_matches_oracle_exactly(gpu_ctx):
+    x, ms, _ = synthetic.workload("aniso_100k_d64", n=20000)
+    got = gpu_ctx.fit_core(x, ms)
+    assert_fit_equal(got, O.fit_core(x, ms))
