@@ -43,6 +43,7 @@ SIGNATURES = {
                                   _F32P, _F32P, _U32P, _U32P, _F32P, _I64P, _VP]),
     "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                          _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
+    "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_clusters_from_spanning_tree": (C.c_int, [_U32P, _U32P, _F64P, C.c_int64, _VP,
                                                      C.POINTER(_VP), C.c_char_p, C.c_size_t]),
     "cuscan_clustering_points": (C.c_int64, [_VP]),
@@ -190,6 +191,9 @@ class Context:
                                                     precision, knn_ids, knn_sq, core_sq, src,
                                                     dst, wsq, C.byref(m), C.byref(stats), stream))
         return int(m.value), stats
+
+    def debug_screen_tile(self, data, n, d, tile_out, stream=None):
+        self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out, stream))
 
     # ---- host-pointer fit ----
     def fit_core(self, x: np.ndarray, min_samples: int, precision: int = PRECISION_PLAIN):

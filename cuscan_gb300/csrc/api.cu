@@ -22,7 +22,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
                        int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
                        int64_t *fallback_rows);
 int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
-                              cudaStream_t s, int64_t *refined_rows);
+                              cudaStream_t s, int64_t *fallback_rows);
+int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
+                      float *out, cudaStream_t s);
 
 }  // namespace cuscan
 
@@ -243,7 +245,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if ((rc = launch_fill_u64(ctx, row_keys, n, ~0ull, s))) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[4], s));
         if (precision == CUSCAN_PRECISION_BF16_REFINED)
-            rc = launch_candidates_refined(ctx, b, n, d, s, &refined_rows);
+            rc = launch_candidates_refined(ctx, b, n, d, s, &fallback_rows);
         else
             rc = launch_candidates_fp32(ctx, as<float>(b.xp), as<float>(b.corep),
                                         as<int32_t>(b.labp), as<int32_t>(b.perm), n, d, row_keys,
@@ -322,6 +324,19 @@ int cuscan_fit_core(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
     CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
     if (n_edges) *n_edges = m;
     return CUSCAN_OK;
+}
+
+int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                             float *tile_out, void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n < 256 || d <= 0 || !data || !tile_out)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "debug tile needs n >= 256 rows");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    int rc = forest_reserve(ctx, ctx->fit->forest, n, d);
+    if (rc) return rc;
+    return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, tile_out, s);
 }
 
 }  // extern "C"

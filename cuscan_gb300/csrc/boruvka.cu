@@ -74,13 +74,14 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
     const float *__restrict__ data, const float *__restrict__ core,
     const int32_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n, int d,
     const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t ref_chunk,
-    unsigned long long *__restrict__ row_keys) {
+    unsigned long long *__restrict__ row_keys, const int32_t *__restrict__ qmap, int64_t nq) {
     extern __shared__ __align__(16) float smem[];
     float *qs = smem;                       // [d][QB]
     float *tiles = smem + (size_t)d * QB;   // 2 x [d][RTP]
     __shared__ float core_t[2][RT];
     __shared__ int32_t lab_t[2][RT];
     __shared__ int32_t id_t[2][RT];
+    __shared__ int32_t q_range[2];
     const int tid = threadIdx.x;
     const int64_t q0 = (int64_t)blockIdx.x * QB;
     const int64_t qi = q0 + tid;
@@ -88,26 +89,30 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
     int64_t r_end = r_begin + ref_chunk;
     if (r_end > n) r_end = n;
 
-    // label range of this block's queries (QB = 4 tiles)
-    int32_t qlo = INT32_MAX, qhi = INT32_MIN;
-    for (int t = 0; t < QB / RT; ++t) {
-        int64_t tt = q0 / RT + t;
-        if (tt * RT < n) {
-            qlo = min(qlo, tile_lo[tt]);
-            qhi = max(qhi, tile_hi[tt]);
-        }
+    // query rows are positions qmap[qi] (or qi) of the same arrays
+    const bool q_valid = qi < nq;
+    const int64_t qpos = q_valid ? (qmap ? (int64_t)qmap[qi] : qi) : 0;
+    const int32_t my_label = q_valid ? labels[qpos] : -1;
+    const float my_core = q_valid ? core[qpos] : 0.0f;
+    if (tid == 0) {
+        q_range[0] = INT32_MAX;
+        q_range[1] = INT32_MIN;
     }
-    const bool q_uniform = qlo == qhi;
-
+    __syncthreads();
+    if (q_valid) {
+        atomicMin(&q_range[0], my_label);
+        atomicMax(&q_range[1], my_label);
+    }
     for (int e = tid; e < QB * d; e += QB) {
         int q = e / d;
         int f = e - q * d;
         int64_t row = q0 + q;
-        qs[f * QB + q] = row < n ? data[row * (int64_t)d + f] : 0.0f;
+        int64_t src = row < nq ? (qmap ? (int64_t)qmap[row] : row) : 0;
+        qs[f * QB + q] = row < nq ? data[src * (int64_t)d + f] : 0.0f;
     }
-    const bool q_valid = qi < n;
-    const int32_t my_label = q_valid ? labels[qi] : -1;
-    const float my_core = q_valid ? core[qi] : 0.0f;
+    __syncthreads();
+    const int32_t qlo = q_range[0], qhi = q_range[1];
+    const bool q_uniform = qlo == qhi;
     unsigned long long best = ~0ull;
 
     auto skip_tile = [&](int64_t r0) -> bool {
@@ -173,7 +178,7 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
         r0 = nxt;
     }
     if (q_valid && best != ~0ull) {
-        const int32_t out = ids ? ids[qi] : (int32_t)qi;
+        const int32_t out = ids ? ids[qpos] : (int32_t)qpos;
         atomicMin(&row_keys[out], best);
     }
 }
@@ -289,14 +294,24 @@ __global__ void reduce_components_kernel(const float *__restrict__ weights,
 
 }  // namespace
 
+int launch_tile_ranges(cuscan_ctx *ctx, const int32_t *labels, int64_t n, int32_t *tile_lo,
+                       int32_t *tile_hi, cudaStream_t s) {
+    const int64_t tiles = ceil_div(n, RT);
+    CUSCAN_KERNEL(tile_range_kernel, (unsigned)ceil_div(tiles, 256), 256, 0, s, labels, n,
+                  tile_lo, tile_hi);
+    CUSCAN_LAUNCH(ctx, "tile_range_kernel");
+    return CUSCAN_OK;
+}
+
 int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core_sq,
                            const int32_t *labels, const int32_t *ids, int64_t n, int d,
                            unsigned long long *row_keys, int32_t *tile_lo, int32_t *tile_hi,
-                           cudaStream_t s) {
-    const int64_t tiles = ceil_div(n, RT);
-    CUSCAN_KERNEL(tile_range_kernel, (unsigned)ceil_div(tiles, 256), 256, 0, s, labels, n, tile_lo, tile_hi);
-    CUSCAN_LAUNCH(ctx, "tile_range_kernel");
-    const int64_t qblocks = ceil_div(n, QB);
+                           cudaStream_t s, const int32_t *qmap, int64_t nq) {
+    if (!qmap) nq = n;
+    if (nq == 0) return CUSCAN_OK;
+    int rc = launch_tile_ranges(ctx, labels, n, tile_lo, tile_hi, s);
+    if (rc) return rc;
+    const int64_t qblocks = ceil_div(nq, QB);
     int64_t splits = 1;
     const int64_t target = 2 * (int64_t)ctx->sm_count;
     if (qblocks < target) splits = ceil_div(target, qblocks);
@@ -314,8 +329,8 @@ int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core
     CUSCAN_CUDA(ctx, cudaFuncSetAttribute(candidates_fp32_kernel,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)qblocks, (unsigned)splits);
-    CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d, tile_lo,
-                                                   tile_hi, chunk, row_keys);
+    CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d,
+                  tile_lo, tile_hi, chunk, row_keys, qmap, nq);
     CUSCAN_LAUNCH(ctx, "candidates_fp32_kernel");
     return CUSCAN_OK;
 }

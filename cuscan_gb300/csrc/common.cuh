@@ -152,20 +152,27 @@ __device__ __forceinline__ bool numerical_bits(uint32_t bits) {
 // Kernel launchers shared between translation units.
 namespace cuscan {
 
-// kNN (knn.cu). All pointers are device pointers.
+// kNN (knn.cu). All pointers are device pointers. With qmap (squared, k <= 32 only), query row
+// i is row qmap[i] of `query`, excludes reference qmap[i] as itself and is written to output
+// row qmap[i].
 int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref,
                           int64_t nr, int d, int k, int exclude_self, int64_t query_offset,
                           int squared, int32_t *ids, float *dist, cudaStream_t s,
-                          Buffer &scratch_ids, Buffer &scratch_dist);
+                          Buffer &scratch_ids, Buffer &scratch_dist,
+                          const int32_t *qmap = nullptr);
 
 // Borůvka candidates (boruvka.cu): per-row 64-bit keys (weight bits << 32 | reference id),
 // minimised atomically into row_keys[] (which the caller fills with ~0 first). Rows are
 // positions in `data`; ids maps a position to the original id used for tie-breaking and
 // output (NULL = identity). tile_lo/tile_hi are scratch of ceil(n/32) ints each.
+// With qmap, only the nq query positions qmap[0..nq) are scanned (against all n positions).
 int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core_sq,
                            const int32_t *labels, const int32_t *ids, int64_t n, int d,
                            unsigned long long *row_keys, int32_t *tile_lo, int32_t *tile_hi,
-                           cudaStream_t s);
+                           cudaStream_t s, const int32_t *qmap = nullptr, int64_t nq = 0);
+// Label range (min, max) of every 32-row tile of `labels`.
+int launch_tile_ranges(cuscan_ctx *ctx, const int32_t *labels, int64_t n, int32_t *tile_lo,
+                       int32_t *tile_hi, cudaStream_t s);
 int launch_fill_u64(cuscan_ctx *ctx, unsigned long long *p, int64_t n, unsigned long long v,
                     cudaStream_t s);
 int launch_keys_to_candidates(cuscan_ctx *ctx, const unsigned long long *keys, int64_t n,

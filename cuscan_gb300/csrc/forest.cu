@@ -523,6 +523,10 @@ void forest_release(ForestBuffers &b) {
                      &b.tile_lo, &b.tile_hi, &b.status_buf, &b.scan_tmp, &b.knn_ids_tmp,
                      &b.knn_dist_tmp};
     for (Buffer *p : all) release(*p);
+    RefinedBuffers &r = b.refined;
+    Buffer *rall[] = {&r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo, &r.tile_hi,
+                      &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error};
+    for (Buffer *p : rall) release(*p);
     b.status = nullptr;
 }
 

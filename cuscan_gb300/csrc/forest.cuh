@@ -14,6 +14,12 @@ struct DevStatus {
     int pad[3];
 };
 
+// Buffers of the bf16 screening path (refined.cu).
+struct RefinedBuffers {
+    Buffer xt, pnorm, mnorm, tile_mmax, tile_lo, tile_hi, cand_ids, cand_lb, fallback, count;
+    Buffer error;
+};
+
 struct ForestBuffers {
     Buffer next, esrc, edst, ew;            // proposals per node
     Buffer jmp_a, mx_a, jmp_b, mx_b;        // pointer doubling
@@ -24,6 +30,7 @@ struct ForestBuffers {
     Buffer tile_lo, tile_hi;                // label range per 32-row tile
     Buffer status_buf, scan_tmp;
     Buffer knn_ids_tmp, knn_dist_tmp;       // split-kNN partial lists
+    RefinedBuffers refined;
     DevStatus *status = nullptr;
 };
 

@@ -75,7 +75,8 @@ template <int K>
 __global__ void __launch_bounds__(QB) knn_fp32_kernel(
     const float *__restrict__ query, int64_t nq, const float *__restrict__ ref, int64_t nr, int d,
     int k, int exclude_self, int64_t query_offset, float pad, int64_t ref_chunk,
-    int32_t *__restrict__ out_ids, float *__restrict__ out_dist, int64_t out_split_stride) {
+    int32_t *__restrict__ out_ids, float *__restrict__ out_dist, int64_t out_split_stride,
+    const int32_t *__restrict__ qmap) {
     extern __shared__ __align__(16) float smem[];
     float *qs = smem;                         // [d][QB]
     float *tiles = smem + (size_t)d * QB;     // 2 x [d][RTP]
@@ -86,12 +87,13 @@ __global__ void __launch_bounds__(QB) knn_fp32_kernel(
     int64_t r_end = r_begin + ref_chunk;
     if (r_end > nr) r_end = nr;
 
-    // stage this block's queries transposed
+    // stage this block's queries transposed (qmap selects a subset of query rows)
     for (int e = tid; e < QB * d; e += QB) {
         int q = e / d;
         int f = e - q * d;
         int64_t row = q0 + q;
-        qs[f * QB + q] = row < nq ? query[row * (int64_t)d + f] : 0.0f;
+        int64_t src = row < nq ? (qmap ? (int64_t)qmap[row] : row) : 0;
+        qs[f * QB + q] = row < nq ? query[src * (int64_t)d + f] : 0.0f;
     }
 
     float ld[K];
@@ -101,7 +103,8 @@ __global__ void __launch_bounds__(QB) knn_fp32_kernel(
         ld[s] = pad;
         li[s] = (int)nr;
     }
-    const int64_t self = exclude_self ? query_offset + qi : -1;
+    const int64_t self =
+        exclude_self ? (qmap ? (qi < nq ? (int64_t)qmap[qi] : -1) : query_offset + qi) : -1;
 
     const int tile_floats = d * RTP;
     int buf = 0;
@@ -149,8 +152,10 @@ __global__ void __launch_bounds__(QB) knn_fp32_kernel(
         buf ^= 1;
     }
     if (qi < nq) {
-        int32_t *oi = out_ids + (int64_t)blockIdx.y * out_split_stride + qi * k;
-        float *od = out_dist + (int64_t)blockIdx.y * out_split_stride + qi * k;
+        // partial lists (split > 1) stay compact; final rows go to their mapped row
+        const int64_t orow = (qmap && out_split_stride == 0) ? (int64_t)qmap[qi] : qi;
+        int32_t *oi = out_ids + (int64_t)blockIdx.y * out_split_stride + orow * k;
+        float *od = out_dist + (int64_t)blockIdx.y * out_split_stride + orow * k;
 #pragma unroll
         for (int s = 0; s < K; ++s) {
             if (s < k) {
@@ -166,9 +171,11 @@ template <int K>
 __global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
                                  const float *__restrict__ part_dist, int64_t nq, int k,
                                  int splits, int64_t split_stride, float pad, int64_t nr,
-                                 int squared, int32_t *__restrict__ ids, float *__restrict__ dist) {
+                                 int squared, int32_t *__restrict__ ids, float *__restrict__ dist,
+                                 const int32_t *__restrict__ qmap) {
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
+    const int64_t orow = qmap ? (int64_t)qmap[q] : q;
     float ld[K];
     int li[K];
 #pragma unroll
@@ -188,9 +195,9 @@ __global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
 #pragma unroll
     for (int s = 0; s < K; ++s) {
         if (s < k) {
-            ids[q * k + s] = li[s];
+            ids[orow * k + s] = li[s];
             float x = ld[s];
-            dist[q * k + s] = squared ? x : sqrtf(x);
+            dist[orow * k + s] = squared ? x : sqrtf(x);
         }
     }
 }
@@ -273,7 +280,7 @@ __global__ void __launch_bounds__(QB) knn_fp32_wide_kernel(
 template <int K>
 int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, int64_t nr, int d,
             int k, int exclude_self, int64_t query_offset, int squared, int32_t *ids, float *dist,
-            cudaStream_t s, Buffer &scratch_ids, Buffer &scratch_dist) {
+            cudaStream_t s, Buffer &scratch_ids, Buffer &scratch_dist, const int32_t *qmap) {
     const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
     const int64_t qblocks = ceil_div(nq, QB);
     // Split the reference range when the query blocks alone cannot fill the GPU.
@@ -291,10 +298,11 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)qblocks, (unsigned)splits);
     if (splits == 1) {
-        CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k, exclude_self,
-                                                   query_offset, pad, chunk, ids, dist, 0);
+        CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k,
+                      exclude_self, query_offset, pad, chunk, ids, dist, 0, qmap);
         CUSCAN_LAUNCH(ctx, "knn_fp32_kernel");
         if (!squared && nq * k > 0) {
+            if (qmap) return fail(ctx, CUSCAN_INVALID_INPUT, "row-subset kNN is squared only");
             CUSCAN_KERNEL(sqrt_rows_kernel, (unsigned)ceil_div(nq * k, 256), 256, 0, s, dist, nq * k);
             CUSCAN_LAUNCH(ctx, "sqrt_rows_kernel");
         }
@@ -305,13 +313,13 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
     if (rc) return rc;
     rc = ensure(ctx, scratch_dist, (size_t)(stride * splits) * sizeof(float), "kNN partial distances");
     if (rc) return rc;
-    CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k, exclude_self, query_offset,
-                                               pad, chunk, as<int32_t>(scratch_ids),
-                                               as<float>(scratch_dist), stride);
+    CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k, exclude_self,
+                  query_offset, pad, chunk, as<int32_t>(scratch_ids), as<float>(scratch_dist),
+                  stride, qmap);
     CUSCAN_LAUNCH(ctx, "knn_fp32_kernel");
-    CUSCAN_KERNEL(knn_merge_kernel<K>, (unsigned)ceil_div(nq, 128), 128, 0, s, 
-        as<int32_t>(scratch_ids), as<float>(scratch_dist), nq, k, (int)splits, stride, pad, nr,
-        squared, ids, dist);
+    CUSCAN_KERNEL(knn_merge_kernel<K>, (unsigned)ceil_div(nq, 128), 128, 0, s,
+                  as<int32_t>(scratch_ids), as<float>(scratch_dist), nq, k, (int)splits, stride,
+                  pad, nr, squared, ids, dist, qmap);
     CUSCAN_LAUNCH(ctx, "knn_merge_kernel");
     return CUSCAN_OK;
 }
@@ -321,22 +329,23 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
 int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref,
                           int64_t nr, int d, int k, int exclude_self, int64_t query_offset,
                           int squared, int32_t *ids, float *dist, cudaStream_t s,
-                          Buffer &scratch_ids, Buffer &scratch_dist) {
+                          Buffer &scratch_ids, Buffer &scratch_dist, const int32_t *qmap) {
     if (nq == 0) return CUSCAN_OK;
     const size_t smem_needed = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
     if (smem_needed > 200 * 1024)
         return fail(ctx, CUSCAN_CAPACITY,
                     "feature count %d exceeds the shared-memory staging limit of the kNN kernel "
-                    "(at most 320 features)", d);
+                    "(at most 256 features)", d);
     if (k <= 8)
         return run_knn<8>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared, ids,
-                          dist, s, scratch_ids, scratch_dist);
+                          dist, s, scratch_ids, scratch_dist, qmap);
     if (k <= 16)
         return run_knn<16>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared,
-                           ids, dist, s, scratch_ids, scratch_dist);
+                           ids, dist, s, scratch_ids, scratch_dist, qmap);
     if (k <= 32)
         return run_knn<32>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared,
-                           ids, dist, s, scratch_ids, scratch_dist);
+                           ids, dist, s, scratch_ids, scratch_dist, qmap);
+    if (qmap) return fail(ctx, CUSCAN_CAPACITY, "row-subset kNN supports k <= 32");
     const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
     const size_t smem = ((size_t)d * QB + (size_t)d * RTP) * sizeof(float);
     CUSCAN_CUDA(ctx, cudaFuncSetAttribute(knn_fp32_wide_kernel,

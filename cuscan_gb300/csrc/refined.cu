@@ -1,20 +1,855 @@
-// bf16 tensor-core screening sweeps with exact f32 re-evaluation (placeholder until the
-// tcgen05 kernels land; the fit rejects the refined precision while this reports 0).
+// bf16 tensor-core screening of the distance sweeps, with exact f32 re-evaluation.
+//
+// The kNN sweep and every Borůvka round first run a screening pass on the 5th-generation tensor
+// cores: the points are rounded to bf16 once, in a pre-swizzled tiled copy, and one persistent
+// CTA per SM computes 128 x 256 tiles of dot products with tcgen05.mma (fp32 accumulators in
+// TMEM, operands streamed into shared memory by bulk async copies). From each dot product the
+// epilogue forms a proven LOWER bound of the reference's f32 squared distance,
+//
+//     L_ij = (1 - C_B)(p_i + p_j) - 2 dot_ij - C_A m_i m_j  <=  d2_ij (sequential-FMA f32),
+//
+// where p = ||x||^2 (f32), m >= ||x||, C_A bounds the bf16 rounding of both operands and the
+// tensor-core accumulation, and C_B the f32 rounding of norms, of the reference sum and of the
+// epilogue arithmetic (see error_coefficients below). Per query row the M smallest bounds (for
+// Borůvka: max(L, core_i, core_j) over other components) stay in registers. A second kernel
+// re-evaluates those M candidates with the exact f32 direct-difference arithmetic and checks the
+// result against the M-th bound: every pair outside the list has a lower bound >= that bound, so
+// when it is larger than the selected exact value no outside pair can change the result. Rows
+// that fail the check are re-run by the exact f32 kernels. The outputs are therefore bit
+// identical to the plain path.
+#include <cuda_bf16.h>
+
+#include <cmath>
+
 #include "common.cuh"
 #include "forest.cuh"
 
 namespace cuscan {
 
-int refined_available() { return 0; }
+namespace {
 
-int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &, const float *, int64_t, int, int,
-                       int32_t *, float *, cudaStream_t, int64_t *, int64_t *) {
-    return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE, "bf16-refined kNN is not built");
+constexpr int BM = 128;            // query rows per block = TMEM lanes
+constexpr int BN = 256;            // reference rows per tile = MMA N
+constexpr int EPI_WARPS = 4;
+constexpr int THREADS = (2 + EPI_WARPS) * 32;
+constexpr uint32_t KBLOCK_A = BM * 128;   // bytes of one 64-element K block of A (16 KiB)
+constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of B (32 KiB)
+constexpr uint32_t WAIT_POLLS = 1u << 22; // bounded mbarrier waits (seconds at most)
+constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
+
+struct Params {
+    const uint8_t *xt;        // bf16 tiles, pre-swizzled (see tile_bf16_kernel)
+    const float *pnorm;       // [n_pad] f32 squared norms (+inf on padding rows)
+    const float *mnorm;       // [n_pad] norms rounded up (0 on padding rows)
+    const float *core;        // [n] core distances (Borůvka)
+    const int32_t *label;     // [n] component labels (Borůvka)
+    const float *tile_mmax;   // [n_tiles] max m over each 256-row tile
+    const int32_t *chunk_lo;  // [ceil(n/32)] label range of 32-row chunks (Borůvka)
+    const int32_t *chunk_hi;
+    const int32_t *tile_lo;   // [n_tiles] label range of 256-row tiles (Borůvka)
+    const int32_t *tile_hi;
+    int64_t n, n_tiles, n_qblocks, n_chunks;
+    int kblocks, stages;
+    float c_a, one_minus_cb;
+    int32_t *cand_ids;        // [n][M]
+    float *cand_lb;           // [n][M]
+    int *error;
+    float *debug_tile;        // when set: CTA 0 writes its first raw 128 x 256 accumulator tile
+};
+
+// ---- PTX wrappers ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: returns false (and raises the CTA abort flag) when the barrier does not flip
+// within WAIT_POLLS polls, or as soon as another role has aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                          int *error) {
+    for (uint32_t it = 0; it < WAIT_POLLS; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *abort) return false;
+    }
+    *abort = 1;
+    atomicExch(error, 1);
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
+    d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;            // SWIZZLE_128B
+    return d;
+}
+// Instruction descriptor: kind::f16, A/B bf16, D f32, both K-major, M=128, N=256.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &, int64_t, int, cudaStream_t,
-                              int64_t *) {
-    return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE, "bf16-refined candidates are not built");
+// Byte offset of element (row r, feature f) in the tiled bf16 copy: 256-row tiles, each split
+// into 64-feature K blocks of 256 rows x 128 bytes whose 16-byte chunks are XOR-swizzled by the
+// row (the SWIZZLE_128B K-major layout), so one bulk copy lands a block ready for the MMA.
+__host__ __device__ __forceinline__ uint64_t tiled_offset(int64_t r, int f, int d_pad) {
+    const int64_t t = r >> 8;
+    const int rr = (int)(r & 255);
+    const int kb = f >> 6, c = f & 63;
+    const int chunk = (c >> 3) ^ (rr & 7);
+    return (uint64_t)t * (uint64_t)(BN * d_pad * 2) + (uint64_t)kb * KBLOCK_B +
+           (uint64_t)rr * 128 + (uint64_t)chunk * 16 + (uint64_t)(c & 7) * 2;
+}
+
+__global__ void tile_bf16_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
+                                 int64_t n_pad, uint8_t *__restrict__ xt) {
+    // one thread per (row, group of 8 features): 16 bytes out
+    const int groups = d_pad >> 3;
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_pad * groups) return;
+    int64_t r = e / groups;
+    int g = (int)(e - r * groups);
+    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        int f = g * 8 + q;
+        float v = (r < n && f < d) ? x[r * d + f] : 0.0f;
+        h[q] = __float2bfloat16_rn(v);
+    }
+    *reinterpret_cast<uint4 *>(xt + tiled_offset(r, g * 8, d_pad)) =
+        *reinterpret_cast<const uint4 *>(h);
+}
+
+__global__ void norms_kernel(const float *__restrict__ x, int64_t n, int d, int64_t n_pad,
+                             float *__restrict__ pnorm, float *__restrict__ mnorm) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_pad) return;
+    if (r >= n) {
+        pnorm[r] = CUSCAN_INF;
+        mnorm[r] = 0.0f;
+        return;
+    }
+    float acc = 0.0f;
+    for (int f = 0; f < d; ++f) {
+        float v = x[r * d + f];
+        acc = __fmaf_rn(v, v, acc);
+    }
+    pnorm[r] = acc;
+    // rounded-up norm, widened by 2^-20 so it bounds the true norm despite the f32 sum
+    mnorm[r] = __fmul_ru(__fsqrt_ru(acc), 1.0f + 0x1p-20f);
+}
+
+__global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t *__restrict__ chunk_lo,
+                                  const int32_t *__restrict__ chunk_hi, int64_t n_tiles,
+                                  int64_t n_chunks, float *__restrict__ tile_mmax,
+                                  int32_t *__restrict__ tile_lo, int32_t *__restrict__ tile_hi) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    float mx = 0.0f;
+    for (int r = 0; r < BN; ++r) mx = fmaxf(mx, mnorm[t * BN + r]);
+    tile_mmax[t] = mx;
+    if (chunk_lo) {
+        int32_t lo = INT32_MAX, hi = INT32_MIN;
+        for (int64_t c = t * 8; c < t * 8 + 8 && c < n_chunks; ++c) {
+            lo = min(lo, chunk_lo[c]);
+            hi = max(hi, chunk_hi[c]);
+        }
+        tile_lo[t] = lo;
+        tile_hi[t] = hi;
+    }
+}
+
+// Label range of query block qb (4 chunks of 32 rows).
+__device__ __forceinline__ void qblock_range(const Params &P, int64_t qb, int32_t &lo,
+                                             int32_t &hi) {
+    lo = INT32_MAX;
+    hi = INT32_MIN;
+    for (int64_t c = qb * 4; c < qb * 4 + 4 && c < P.n_chunks; ++c) {
+        lo = min(lo, P.chunk_lo[c]);
+        hi = max(hi, P.chunk_hi[c]);
+    }
+}
+
+template <bool BORUVKA>
+__device__ __forceinline__ bool tile_skipped(const Params &P, int64_t t, int32_t qlo, int32_t qhi) {
+    if (!BORUVKA) return false;
+    return qlo == qhi && P.tile_lo[t] == qlo && P.tile_hi[t] == qlo;
+}
+
+template <int M>
+__device__ __forceinline__ void list_insert(float (&L)[M], int (&J)[M], float x, int j) {
+#pragma unroll
+    for (int s = M - 1; s >= 0; --s) {
+        const bool here = x < L[s];
+        const bool prev = (s > 0) ? (x < L[s > 0 ? s - 1 : 0]) : false;
+        if (here) {
+            if (prev) {
+                L[s] = L[s > 0 ? s - 1 : 0];
+                J[s] = J[s > 0 ? s - 1 : 0];
+            } else {
+                L[s] = x;
+                J[s] = j;
+            }
+        }
+    }
+}
+
+template <int M, bool BORUVKA>
+__global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t a_bytes = (uint32_t)P.kblocks * KBLOCK_A;
+    const uint32_t b_bytes = (uint32_t)P.kblocks * KBLOCK_B;
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + a_bytes;
+    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][2][BN]
+    float *vstage = pbuf + EPI_WARPS * 2 * BN;                       // [EPI_WARPS][32][VSTRIDE]
+    uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
+    uint64_t *full = bars;
+    uint64_t *empty = bars + P.stages;
+    uint64_t *a_full = bars + 2 * P.stages;
+    uint64_t *a_empty = a_full + 1;
+    uint64_t *t_full = a_full + 2;   // [2]
+    uint64_t *t_empty = a_full + 4;  // [2]
+    uint64_t *done = a_full + 6;     // MMA drain on the abort path
+    uint32_t *tmem_slot = (uint32_t *)(a_full + 7);
+    volatile int *abort = (volatile int *)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < P.stages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(a_full, 1);
+        mbar_init(a_empty, 1);
+        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&t_full[b], 1);
+            mbar_init(&t_empty[b], EPI_WARPS);
+        }
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                         smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- producer: bulk copies of A (per query block) and B tiles ----------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, a_phase = 0;
+            // parity of the last fill of each stage (bit 1 set = a fill was issued)
+            uint32_t issued[4] = {0, 0, 0, 0};
+            uint32_t a_issued = 0;
+            for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+                if (!mbar_wait(a_empty, a_phase ^ 1, abort, P.error)) break;
+                a_issued = 2u | a_phase;
+                a_phase ^= 1;
+                mbar_expect_tx(a_full, a_bytes);
+                const uint8_t *asrc = P.xt + (uint64_t)(qb >> 1) * (uint64_t)b_bytes +
+                                      (uint64_t)(qb & 1) * KBLOCK_A;
+                for (int kb = 0; kb < P.kblocks; ++kb)
+                    bulk_g2s(sA + kb * KBLOCK_A, asrc + (uint64_t)kb * KBLOCK_B, KBLOCK_A, a_full);
+                int32_t qlo = 0, qhi = 0;
+                if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+                for (int64_t t = 0; t < P.n_tiles; ++t) {
+                    if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
+                    if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
+                    issued[stage] = 2u | phase;
+                    mbar_expect_tx(&full[stage], b_bytes);
+                    const uint8_t *bsrc = P.xt + (uint64_t)t * (uint64_t)b_bytes;
+                    uint8_t *bdst = sB + (size_t)stage * b_bytes;
+                    for (int kb = 0; kb < P.kblocks; ++kb)
+                        bulk_g2s(bdst + kb * KBLOCK_B, bsrc + (uint64_t)kb * KBLOCK_B, KBLOCK_B,
+                                 &full[stage]);
+                    if (++stage == P.stages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            if (*abort) {
+                // let every copy this thread issued land before the CTA exits
+                for (int s2 = 0; s2 < P.stages; ++s2)
+                    if (issued[s2]) {
+                        for (uint32_t it = 0; it < WAIT_POLLS; ++it)
+                            if (mbar_try_wait(&full[s2], issued[s2] & 1u)) break;
+                    }
+                if (a_issued)
+                    for (uint32_t it = 0; it < WAIT_POLLS; ++it)
+                        if (mbar_try_wait(a_full, a_issued & 1u)) break;
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer: one thread -------------------------------------------
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0, a_phase = 0;
+            uint32_t tcount = 0, a_commits = 0;
+            const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
+            for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+                if (!mbar_wait(a_full, a_phase, abort, P.error)) break;
+                a_phase ^= 1;
+                fence_after();
+                int32_t qlo = 0, qhi = 0;
+                if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+                bool ok = true;
+                for (int64_t t = 0; t < P.n_tiles; ++t) {
+                    if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
+                    const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
+                    if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
+                    fence_after();
+                    if (!mbar_wait(&full[stage], phase, abort, P.error)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d_tmem = tmem_base + b * BN;
+                    const uint32_t bstage = b_base + (uint32_t)stage * b_bytes;
+                    for (int kb = 0; kb < P.kblocks; ++kb) {
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks) {
+                            const uint64_t ad = desc_sw128(a_base + kb * KBLOCK_A + ks * 32);
+                            const uint64_t bd = desc_sw128(bstage + kb * KBLOCK_B + ks * 32);
+                            mma_bf16(d_tmem, ad, bd, (kb | ks) != 0);
+                        }
+                    }
+                    mma_commit(&empty[stage]);
+                    mma_commit(&t_full[b]);
+                    if (++stage == P.stages) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                    ++tcount;
+                }
+                mma_commit(a_empty);
+                ++a_commits;
+                if (!ok) break;
+            }
+            // wait until every issued MMA has completed before TMEM can be released
+            mma_commit(done);
+            for (uint32_t it = 0; it < WAIT_POLLS; ++it)
+                if (mbar_try_wait(done, 0)) break;
+            if (a_commits)
+                for (uint32_t it = 0; it < WAIT_POLLS; ++it)
+                    if (mbar_try_wait(a_empty, (a_commits - 1) & 1u)) break;
+        }
+    } else {
+        // ---------------- epilogue: one thread per query row --------------------------------
+        const int ew = warp - 2;              // 0..3
+        const int quad = warp & 3;            // TMEM lane quadrant of this warp
+        const int row_local = quad * 32 + lane;
+        float *my_pbuf = pbuf + ew * 2 * BN;
+        float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
+        uint32_t tcount = 0;
+        for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+            const int64_t row = qb * BM + row_local;
+            const bool valid = row < P.n;
+            const float p_i = valid ? P.pnorm[row] : 0.0f;
+            const float m_i = valid ? P.mnorm[row] : 0.0f;
+            const float ps_i = P.one_minus_cb * p_i;
+            const float cm_i = P.c_a * m_i;
+            float core_i = 0.0f;
+            int32_t lab_i = -1;
+            if (BORUVKA && valid) {
+                core_i = P.core[row];
+                lab_i = P.label[row];
+            }
+            float L[M];
+            int J[M];
+#pragma unroll
+            for (int s = 0; s < M; ++s) {
+                L[s] = CUSCAN_INF;
+                J[s] = -1;
+            }
+            int32_t qlo = 0, qhi = 0;
+            if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+            bool ok = true;
+            for (int64_t t = 0; t < P.n_tiles; ++t) {
+                if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
+                const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
+                // stage the scaled column norms of this tile for the fast test
+                float *pb = my_pbuf + b * BN;
+                {
+                    const float4 *src = reinterpret_cast<const float4 *>(P.pnorm + t * BN);
+                    float4 v0 = src[lane * 2], v1 = src[lane * 2 + 1];
+                    const float s = P.one_minus_cb;
+                    v0.x *= s; v0.y *= s; v0.z *= s; v0.w *= s;
+                    v1.x *= s; v1.y *= s; v1.z *= s; v1.w *= s;
+                    reinterpret_cast<float4 *>(pb)[lane * 2] = v0;
+                    reinterpret_cast<float4 *>(pb)[lane * 2 + 1] = v1;
+                }
+                __syncwarp();
+                const float mt = P.tile_mmax[t];
+                if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
+                fence_after();
+                const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN;
+                for (int c = 0; c < BN / 32; ++c) {
+                    float v[32];
+                    tmem_ld32(taddr + c * 32, v);
+                    if (P.debug_tile && blockIdx.x == 0 && tcount == 0) {
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) P.debug_tile[row_local * BN + c * 32 + e] = v[e];
+                    }
+                    bool active = valid;
+                    if (BORUVKA) {
+                        const int64_t ch = t * 8 + c;
+                        if (ch >= P.n_chunks) active = false;
+                        else if (P.chunk_lo[ch] == lab_i && P.chunk_hi[ch] == lab_i) active = false;
+                    }
+                    // fast threshold, widened by a few ulps so that the fast test never rejects
+                    // a pair whose exact-path bound would enter the list
+                    const float base = L[M - 1] - ps_i + cm_i * mt;
+                    const float thr2 = base + 0x1p-21f * (fabsf(L[M - 1]) + ps_i + cm_i * mt);
+                    unsigned hits = 0;
+                    if (active) {
+                        const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const float4 pq = pc[q];
+                            hits |= (fmaf(-2.0f, v[4 * q + 0], pq.x) < thr2) ? (1u << (4 * q + 0)) : 0u;
+                            hits |= (fmaf(-2.0f, v[4 * q + 1], pq.y) < thr2) ? (1u << (4 * q + 1)) : 0u;
+                            hits |= (fmaf(-2.0f, v[4 * q + 2], pq.z) < thr2) ? (1u << (4 * q + 2)) : 0u;
+                            hits |= (fmaf(-2.0f, v[4 * q + 3], pq.w) < thr2) ? (1u << (4 * q + 3)) : 0u;
+                        }
+                    }
+                    if (__any_sync(0xffffffffu, hits != 0u)) {
+                        if (hits) {
+#pragma unroll
+                            for (int q = 0; q < 8; ++q)
+                                reinterpret_cast<float4 *>(my_v)[q] =
+                                    make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                        }
+                        while (hits) {
+                            const int e = __ffs(hits) - 1;
+                            hits &= hits - 1;
+                            const int64_t j = t * BN + c * 32 + e;
+                            if (j >= P.n) continue;
+                            if (!BORUVKA && j == row) continue;
+                            const float dot = my_v[e];
+                            // exact lower bound for this pair (per-column norm instead of the
+                            // tile maximum)
+                            const float pj = P.pnorm[j], mj = P.mnorm[j];
+                            float lb = fmaf(-cm_i, mj, fmaf(-2.0f, dot, P.one_minus_cb * pj) + ps_i);
+                            if (BORUVKA) {
+                                if (P.label[j] == lab_i) continue;
+                                lb = fmaxf(fmaxf(lb, core_i), P.core[j]);
+                            }
+                            if (lb < L[M - 1]) list_insert<M>(L, J, lb, (int)j);
+                        }
+                        __syncwarp();
+                    }
+                }
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&t_empty[b]);
+                ++tcount;
+            }
+            if (!ok) break;
+            if (valid) {
+#pragma unroll
+                for (int s = 0; s < M; ++s) {
+                    P.cand_ids[row * M + s] = J[s];
+                    P.cand_lb[row * M + s] = L[s];
+                }
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem_base)
+                     : "memory");
+    }
+}
+
+// Exact f32 squared distance in the reference's order.
+__device__ __forceinline__ float exact_d2(const float *__restrict__ a, const float *__restrict__ b,
+                                          int d) {
+    float acc = 0.0f;
+    for (int f = 0; f < d; ++f) {
+        const float t = a[f] - b[f];
+        acc = __fmaf_rn(t, t, acc);
+    }
+    return acc;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u < v ? u : v;
+    }
+    return v;
+}
+
+// kNN re-rank: one warp per row, exact distances of the M candidates, top-k by (d, id).
+template <int M>
+__global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d, int k,
+                                  const int32_t *__restrict__ cand_ids,
+                                  const float *__restrict__ cand_lb, int32_t *__restrict__ ids,
+                                  float *__restrict__ dist, int32_t *__restrict__ fallback,
+                                  int *__restrict__ fallback_count) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    constexpr int PER = M / 32;
+    unsigned long long key[PER];
+    const float *xr = x + row * d;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int s = q * 32 + lane;
+        const int32_t j = cand_ids[row * M + s];
+        if (j < 0) {
+            key[q] = ~0ull;
+        } else {
+            const float dd = exact_d2(xr, x + (int64_t)j * d, d);
+            key[q] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)j;
+        }
+    }
+    float dk = CUSCAN_INF;
+    for (int r = 0; r < k; ++r) {
+        unsigned long long mine = key[0];
+#pragma unroll
+        for (int q = 1; q < PER; ++q) mine = key[q] < mine ? key[q] : mine;
+        const unsigned long long best = warp_min_u64(mine);
+#pragma unroll
+        for (int q = 0; q < PER; ++q)
+            if (key[q] == best) key[q] = ~0ull;
+        if (best == ~0ull) {
+            if (lane == 0) {
+                ids[row * k + r] = (int32_t)n;
+                dist[row * k + r] = CUSCAN_INF;
+            }
+            dk = CUSCAN_INF;
+        } else {
+            dk = __uint_as_float((uint32_t)(best >> 32));
+            if (lane == 0) {
+                ids[row * k + r] = (int32_t)(uint32_t)best;
+                dist[row * k + r] = dk;
+            }
+        }
+    }
+    // every pair outside the list has a lower bound >= the M-th bound
+    const float bound = cand_lb[row * M + M - 1];
+    const bool full = cand_ids[row * M + M - 1] >= 0;
+    if (lane == 0 && full && !(bound > dk)) {
+        const int at = atomicAdd(fallback_count, 1);
+        fallback[at] = (int32_t)row;
+    }
+}
+
+// Borůvka re-rank over component-sorted positions: exact weight of each candidate, row minimum
+// (w, original j) into row_keys[original row].
+template <int M>
+__global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float *__restrict__ corep,
+                                      const int32_t *__restrict__ labp,
+                                      const int32_t *__restrict__ perm, int64_t n, int d,
+                                      const int32_t *__restrict__ cand_ids,
+                                      const float *__restrict__ cand_lb,
+                                      unsigned long long *__restrict__ row_keys,
+                                      int32_t *__restrict__ fallback,
+                                      int *__restrict__ fallback_count) {
+    const int64_t pos = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pos >= n) return;
+    constexpr int PER = M / 32;
+    const float *xr = xp + pos * d;
+    const float ci = corep[pos];
+    const int32_t li = labp[pos];
+    unsigned long long mine = ~0ull;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int32_t j = cand_ids[pos * M + q * 32 + lane];
+        if (j < 0 || labp[j] == li) continue;
+        const float w = fmaxf(fmaxf(exact_d2(xr, xp + (int64_t)j * d, d), ci), corep[j]);
+        if (w != w) continue;
+        const unsigned long long key =
+            ((unsigned long long)weight_key_bits(w) << 32) | (uint32_t)perm[j];
+        mine = key < mine ? key : mine;
+    }
+    const unsigned long long best = warp_min_u64(mine);
+    if (lane == 0) {
+        const float bound = cand_lb[pos * M + M - 1];
+        const bool full = cand_ids[pos * M + M - 1] >= 0;
+        const float wmin = best == ~0ull ? CUSCAN_INF : __uint_as_float((uint32_t)(best >> 32));
+        if (best != ~0ull) row_keys[perm[pos]] = best;
+        if (best == ~0ull || (full && !(bound > wmin))) {
+            const int at = atomicAdd(fallback_count, 1);
+            fallback[at] = (int32_t)pos;
+        }
+    }
+}
+
+// Error bound coefficients for d features (K = padded depth of the bf16 dot product).
+void error_coefficients(int d, int d_pad, float &c_a, float &c_b) {
+    const double u = std::ldexp(1.0, -8);    // bf16 unit roundoff (round to nearest)
+    const double u32 = std::ldexp(1.0, -24); // f32 unit roundoff
+    // bf16 rounding of both factors, plus a generous bound on the tensor-core f32 accumulation
+    // (each of K partial sums off by at most 2^-21 of the running magnitude)
+    const double a1 = (2.0 * u + u * u) + (double)d_pad * std::ldexp(1.0, -21) * (1 + u) * (1 + u);
+    // norms and the reference sum each carry at most (d + 2) f32 roundings; the epilogue adds a
+    // few more; everything is taken three times over
+    const double b = 3.5 * (double)(d + 4) * u32 + 1e-7;
+    c_a = (float)(2.0 * a1 * (1.0 + 1e-4));
+    c_b = (float)b;
+}
+
+}  // namespace
+
+int refined_available() { return 1; }
+
+struct Layout {
+    int d_pad, kblocks, stages;
+    int64_t n_pad, n_tiles, n_qblocks;
+    size_t smem;
+};
+
+static bool refined_layout(int64_t n, int d, Layout &L) {
+    L.d_pad = (int)ceil_div(d, 64) * 64;
+    if (L.d_pad > 128) return false;
+    L.kblocks = L.d_pad / 64;
+    L.n_tiles = ceil_div(n, BN);
+    L.n_pad = L.n_tiles * BN;
+    L.n_qblocks = ceil_div(n, BM);
+    const size_t a = (size_t)L.kblocks * KBLOCK_A, b = (size_t)L.kblocks * KBLOCK_B;
+    const size_t fixed = a + (size_t)EPI_WARPS * 2 * BN * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+                         256 + 1024;
+    int st = (int)((210 * 1024 - fixed) / b);
+    if (st > 4) st = 4;
+    if (st < 2) return false;
+    L.stages = st;
+    L.smem = fixed + (size_t)st * b;
+    return true;
+}
+
+static bool refined_shape_ok(int64_t n, int d, int k) {
+    Layout L;
+    return n >= 2048 && k <= 32 && refined_layout(n, d, L);
+}
+
+static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float *x, int64_t n,
+                int d, const int32_t *chunk_lo, const int32_t *chunk_hi, cudaStream_t s) {
+    int rc = ensure(ctx, R.xt, (size_t)L.n_pad * L.d_pad * 2, "bf16 tiles");
+    if (!rc) rc = ensure(ctx, R.pnorm, sizeof(float) * L.n_pad, "norms");
+    if (!rc) rc = ensure(ctx, R.mnorm, sizeof(float) * L.n_pad, "norms");
+    if (!rc) rc = ensure(ctx, R.tile_mmax, sizeof(float) * L.n_tiles, "tile norms");
+    if (!rc) rc = ensure(ctx, R.tile_lo, sizeof(int32_t) * L.n_tiles, "tile labels");
+    if (!rc) rc = ensure(ctx, R.tile_hi, sizeof(int32_t) * L.n_tiles, "tile labels");
+    if (!rc) rc = ensure(ctx, R.error, 16, "error flag");
+    if (!rc) rc = ensure(ctx, R.count, 16, "fallback count");
+    if (!rc) rc = ensure(ctx, R.fallback, sizeof(int32_t) * n, "fallback rows");
+    if (rc) return rc;
+    const int64_t groups = L.n_pad * (L.d_pad / 8);
+    CUSCAN_KERNEL(tile_bf16_kernel, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d, L.d_pad,
+                  L.n_pad, as<uint8_t>(R.xt));
+    CUSCAN_KERNEL(norms_kernel, (unsigned)ceil_div(L.n_pad, 256), 256, 0, s, x, n, d, L.n_pad,
+                  as<float>(R.pnorm), as<float>(R.mnorm));
+    CUSCAN_KERNEL(tile_stats_kernel, (unsigned)ceil_div(L.n_tiles, 128), 128, 0, s,
+                  as<float>(R.mnorm), chunk_lo, chunk_hi, L.n_tiles, ceil_div(n, 32),
+                  as<float>(R.tile_mmax), as<int32_t>(R.tile_lo), as<int32_t>(R.tile_hi));
+    CUSCAN_LAUNCH(ctx, "refined prep");
+    return CUSCAN_OK;
+}
+
+template <int M, bool BORUVKA>
+static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64_t n, int d,
+                      const float *core, const int32_t *label, const int32_t *chunk_lo,
+                      const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr) {
+    int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * M, "screen candidates");
+    if (!rc) rc = ensure(ctx, R.cand_lb, sizeof(float) * n * M, "screen bounds");
+    if (rc) return rc;
+    Params P{};
+    P.xt = as<uint8_t>(R.xt);
+    P.pnorm = as<float>(R.pnorm);
+    P.mnorm = as<float>(R.mnorm);
+    P.core = core;
+    P.label = label;
+    P.tile_mmax = as<float>(R.tile_mmax);
+    P.chunk_lo = chunk_lo;
+    P.chunk_hi = chunk_hi;
+    P.tile_lo = as<int32_t>(R.tile_lo);
+    P.tile_hi = as<int32_t>(R.tile_hi);
+    P.n = n;
+    P.n_tiles = L.n_tiles;
+    P.n_qblocks = L.n_qblocks;
+    P.n_chunks = ceil_div(n, 32);
+    P.kblocks = L.kblocks;
+    P.stages = L.stages;
+    float ca, cb;
+    error_coefficients(d, L.d_pad, ca, cb);
+    P.c_a = ca;
+    P.one_minus_cb = 1.0f - cb;
+    P.cand_ids = as<int32_t>(R.cand_ids);
+    P.cand_lb = as<float>(R.cand_lb);
+    P.error = as<int>(R.error);
+    P.debug_tile = debug_tile;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
+    auto kernel = screen_kernel<M, BORUVKA>;
+    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)L.smem));
+    int64_t grid = L.n_qblocks < ctx->sm_count ? L.n_qblocks : ctx->sm_count;
+    CUSCAN_KERNEL(kernel, (unsigned)grid, THREADS, L.smem, s, P);
+    CUSCAN_LAUNCH(ctx, "screen_kernel");
+    return CUSCAN_OK;
+}
+
+static int read_screen_status(cuscan_ctx *ctx, RefinedBuffers &R, cudaStream_t s, int &fallbacks) {
+    int host[2] = {0, 0};
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&host[0], R.error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&host[1], R.count.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    if (host[0])
+        return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE,
+                    "tensor-core screening timed out waiting on a pipeline barrier");
+    fallbacks = host[1];
+    return CUSCAN_OK;
+}
+
+int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d, int k,
+                       int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
+                       int64_t *fallback_rows) {
+    if (!refined_shape_ok(n, d, k)) {
+        // shapes outside the tensor-core tiling run the exact f32 sweep
+        return launch_exact_knn_fp32(ctx, x, n, x, n, d, k, 1, 0, 1, ids, dist, s, b.knn_ids_tmp,
+                                     b.knn_dist_tmp);
+    }
+    RefinedBuffers &R = b.refined;
+    Layout L;
+    refined_layout(n, d, L);
+    int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
+    if (rc) return rc;
+    constexpr int M = 32;
+    if ((rc = run_screen<M, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, x, n, d, k,
+                  as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
+                  as<int32_t>(R.fallback), as<int>(R.count));
+    CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
+    int fallbacks = 0;
+    if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
+    if (refined_rows) *refined_rows += n;
+    if (fallback_rows) *fallback_rows += fallbacks;
+    if (fallbacks > 0)
+        return launch_exact_knn_fp32(ctx, x, fallbacks, x, n, d, k, 1, 0, 1, ids, dist, s,
+                                     b.knn_ids_tmp, b.knn_dist_tmp, as<int32_t>(R.fallback));
+    return CUSCAN_OK;
+}
+
+int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
+                              cudaStream_t s, int64_t *fallback_rows) {
+    const float *xp = as<float>(b.xp);
+    const float *corep = as<float>(b.corep);
+    const int32_t *labp = as<int32_t>(b.labp);
+    const int32_t *perm = as<int32_t>(b.perm);
+    unsigned long long *row_keys = as<unsigned long long>(b.row_keys);
+    int32_t *clo = as<int32_t>(b.tile_lo), *chi = as<int32_t>(b.tile_hi);
+    if (!refined_shape_ok(n, d, 1))
+        return launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s);
+    RefinedBuffers &R = b.refined;
+    Layout L;
+    refined_layout(n, d, L);
+    int rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
+    if (!rc) rc = prep(ctx, R, L, xp, n, d, clo, chi, s);
+    if (rc) return rc;
+    constexpr int M = 32;
+    if ((rc = run_screen<M, true>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+    CUSCAN_KERNEL(rerank_boruvka_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xp, corep,
+                  labp, perm, n, d, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), row_keys,
+                  as<int32_t>(R.fallback), as<int>(R.count));
+    CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
+    int fallbacks = 0;
+    if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
+    if (fallback_rows) *fallback_rows += fallbacks;
+    if (fallbacks > 0)
+        return launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s,
+                                      as<int32_t>(R.fallback), fallbacks);
+    return CUSCAN_OK;
+}
+
+int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
+                      float *out, cudaStream_t s) {
+    Layout L;
+    if (!refined_layout(n, d, L))
+        return fail(ctx, CUSCAN_CAPACITY, "shape outside the tensor-core tiling");
+    RefinedBuffers &R = b.refined;
+    int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
+    if (!rc) rc = run_screen<32, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
+    if (rc) return rc;
+    int fallbacks = 0;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+    return read_screen_status(ctx, R, s, fallbacks);
 }
 
 }  // namespace cuscan

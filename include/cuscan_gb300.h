@@ -154,6 +154,15 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
                            float *mst_wsq, int64_t *n_edges, cuscan_fit_stats *stats,
                            void *stream);
 
+/*
+ * Diagnostic of the bf16 tensor-core screen (no reference counterpart): runs the screening
+ * pipeline on `data` (device, n >= 256 rows) and writes the raw fp32 accumulator of the first
+ * 128-row query block against the first 256-row reference tile, i.e. the bf16 dot products
+ * x_r . x_c for r < 128, c < 256, to tile_out[128*256] (device, row-major). Synchronises.
+ */
+int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                             float *tile_out, void *stream);
+
 /* ---- host-side extraction (no device work) ---- */
 
 typedef struct cuscan_extract_config {

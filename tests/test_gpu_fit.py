@@ -16,7 +16,7 @@ from tests.conftest import load_case
 
 pytestmark = pytest.mark.gpu
 
-PRECISIONS = [_lib.PRECISION_PLAIN]
+PRECISIONS = [_lib.PRECISION_PLAIN, _lib.PRECISION_BF16_REFINED]
 
 
 def bits(a):
@@ -163,7 +163,30 @@ def test_full_size_fp32_workload_properties(gpu_ctx):
     check_tree_properties(x, out, ms)
 
 
-def test_medium_workload_matches_oracle_exactly(gpu_ctx):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_medium_workload_matches_oracle_exactly(gpu_ctx, precision):
     x, ms, _ = synthetic.workload("aniso_100k_d64", n=20000)
-    got = gpu_ctx.fit_core(x, ms)
+    got = gpu_ctx.fit_core(x, ms, precision)
     assert_fit_equal(got, O.fit_core(x, ms))
+
+
+def test_refined_vmf_matches_oracle_and_uses_tensor_screen(gpu_ctx):
+    """vMF-like unit vectors (d=128, min_samples=15) at n=30000: the bf16 screen handles the
+    rows and the result equals the oracle bit for bit."""
+    x = synthetic.vmf_like(n=30000, d=128, clusters=40, seed=12)
+    got = gpu_ctx.fit_core(x, 15, _lib.PRECISION_BF16_REFINED)
+    assert got["stats"]["refined_rows"] == x.shape[0]
+    assert got["stats"]["fallback_rows"] < 0.05 * x.shape[0] * (1 + got["stats"]["rounds"])
+    assert_fit_equal(got, O.fit_core(x, 15))
+
+
+def test_full_size_refined_equals_plain(gpu_ctx):
+    """vmf_500k_d128 reduced to n=120000: bf16-refined and plain fits agree bit for bit."""
+    x, ms, _ = synthetic.workload("vmf_500k_d128", n=120000)
+    a = gpu_ctx.fit_core(x, ms, _lib.PRECISION_PLAIN)
+    b = gpu_ctx.fit_core(x, ms, _lib.PRECISION_BF16_REFINED)
+    for key in ("knn_ids", "src", "dst"):
+        np.testing.assert_array_equal(a[key], b[key])
+    for key in ("knn_sq", "core_sq", "wsq"):
+        np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
+    check_tree_properties(x, b, ms)

@@ -174,3 +174,22 @@ def test_component_reduce_matches_oracle(gpu_ctx, n, comps, tile, seed):
     eww, ewm = O.component_reduce(w, dst, plan)
     np.testing.assert_array_equal(wm, ewm)
     np.testing.assert_array_equal(bits(ww), bits(eww))
+
+
+@pytest.mark.parametrize("n,d,seed", [(512, 128, 0), (600, 64, 1), (300, 10, 2), (1000, 100, 3)])
+def test_tensor_core_tile_matches_bf16_products(gpu_ctx, n, d, seed):
+    """The tcgen05 screen's raw accumulator for query rows 0..127 x reference rows 0..255
+    equals the dot products of the bf16-rounded rows (f32 accumulation tolerance)."""
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n, d)).astype(np.float32)
+    tx = dev(x)
+    out = torch.zeros((128, 256), dtype=torch.float32, device="cuda")
+    gpu_ctx.debug_screen_tile(ptr(tx), n, d, ptr(out), stream())
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().astype(np.float64)
+    xb = torch.from_numpy(x).to(torch.bfloat16).to(torch.float64).numpy()
+    cols = min(256, n)
+    exp = xb[:128] @ xb[:cols].T
+    scale = np.abs(xb[:128]) @ np.abs(xb[:cols]).T
+    err = np.abs(got[:, :cols] - exp)
+    assert np.all(err <= 1e-5 * scale + 1e-30), float(np.max(err / np.maximum(scale, 1e-30)))
