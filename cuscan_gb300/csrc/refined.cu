@@ -34,7 +34,8 @@ constexpr int EPI_WARPS = 4;
 constexpr int THREADS = (2 + EPI_WARPS) * 32;
 constexpr uint32_t KBLOCK_A = BM * 128;   // bytes of one 64-element K block of A (16 KiB)
 constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of B (32 KiB)
-constexpr uint32_t WAIT_POLLS = 1u << 22; // bounded mbarrier waits (seconds at most)
+constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded mbarrier waits: 2 s of wall time
+constexpr uint32_t WAIT_POLLS = 1u << 22;      // poll bound of the abort-path drains
 constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
 
 struct Params {
@@ -82,13 +83,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: returns false (and raises the CTA abort flag) when the barrier does not flip
-// within WAIT_POLLS polls, or as soon as another role has aborted.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: returns false (and raises the CTA abort flag and the error word) when the
+// barrier does not flip within WAIT_NS nanoseconds, or as soon as another role has aborted.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           int *error) {
-    for (uint32_t it = 0; it < WAIT_POLLS; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u && *abort) return false;
+        if ((it & 255u) == 0u) {
+            if (*abort) return false;
+            if (global_ns() - t0 > WAIT_NS) break;
+        }
     }
     *abort = 1;
     atomicExch(error, 1);
