@@ -335,6 +335,10 @@ def run_ours(args):
                    "rounds": stats["rounds"], "components_after_seed":
                        stats["components_after_seed"],
                    "core_ms": stats["core_ms"], "mst_ms": stats["mst_ms"],
+                   "knn_kernel_ms": stats["knn_kernel_ms"],
+                   "candidate_kernel_ms": stats["candidate_kernel_ms"],
+                   "knn_fallback_rows": stats["fallback_rows"],
+                   "boruvka_fallback_rows": stats["boruvka_fallback_rows"],
                    "algorithmic_tflop_per_step": (w_knn + w_cand) / 1e12},
         "clocks": clocks.summary(),
         "e2e": {"value": world * n * args.steps / e2e_s / 1e6, "unit": "Mpts/s",

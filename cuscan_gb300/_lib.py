@@ -66,6 +66,7 @@ class FitStats(C.Structure):
         ("components_after_seed", C.c_int64),
         ("refined_rows", C.c_int64),
         ("fallback_rows", C.c_int64),
+        ("boruvka_fallback_rows", C.c_int64),
         ("cross_pairs", C.c_double),
     ]
 

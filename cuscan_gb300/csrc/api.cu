@@ -211,7 +211,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     const int k = (int)((int64_t)min_samples < n - 1 ? min_samples : n - 1);
     int32_t *label = as<int32_t>(f->label);
     cudaEvent_t *ev = f->ev;
-    int64_t refined_rows = 0, fallback_rows = 0;
+    int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0;
 
     CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
@@ -245,7 +245,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if ((rc = launch_fill_u64(ctx, row_keys, n, ~0ull, s))) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[4], s));
         if (precision == CUSCAN_PRECISION_BF16_REFINED)
-            rc = launch_candidates_refined(ctx, b, n, d, s, &fallback_rows);
+            rc = launch_candidates_refined(ctx, b, n, d, s, &boruvka_fallback_rows);
         else
             rc = launch_candidates_fp32(ctx, as<float>(b.xp), as<float>(b.corep),
                                         as<int32_t>(b.labp), as<int32_t>(b.perm), n, d, row_keys,
@@ -276,6 +276,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->components_after_seed = after_seed;
         stats->refined_rows = refined_rows;
         stats->fallback_rows = fallback_rows;
+        stats->boruvka_fallback_rows = boruvka_fallback_rows;
         stats->cross_pairs = cross_pairs;
     }
     return CUSCAN_OK;
