@@ -30,7 +30,8 @@ namespace {
 
 constexpr int BM = 128;            // query rows per block = TMEM lanes
 constexpr int BN = 256;            // reference rows per tile = MMA N
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 8;            // two per TMEM lane quadrant
+constexpr int HALF = 128;                // columns of a tile per epilogue warp
 constexpr int THREADS = (2 + EPI_WARPS) * 32;
 constexpr uint32_t KBLOCK_A = BM * 128;   // bytes of one 64-element K block of A (16 KiB)
 constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of B (32 KiB)
@@ -275,8 +276,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     const uint32_t b_bytes = (uint32_t)P.kblocks * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
-    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][2][BN]
-    float *vstage = pbuf + EPI_WARPS * 2 * BN;                       // [EPI_WARPS][32][VSTRIDE]
+    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][4][HALF]
+    float *vstage = pbuf + EPI_WARPS * 4 * HALF;                     // [EPI_WARPS][32][VSTRIDE]
     uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
     uint64_t *full = bars;
     uint64_t *empty = bars + P.stages;
@@ -415,11 +416,14 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     if (mbar_try_wait(a_empty, (a_commits - 1) & 1u)) break;
         }
     } else {
-        // ---------------- epilogue: one thread per query row --------------------------------
-        const int ew = warp - 2;              // 0..3
+        // ---------------- epilogue: two threads per query row ---------------------------------
+        // Warps 2..9: warp w reads TMEM lane quadrant w % 4 (hardware rule) and handles one half
+        // of every 256-column tile; the two threads of a row keep separate top-M lists.
+        const int ew = warp - 2;              // 0..7
         const int quad = warp & 3;            // TMEM lane quadrant of this warp
+        const int half = ew >> 2;             // column half of each tile
         const int row_local = quad * 32 + lane;
-        float *my_pbuf = pbuf + ew * 2 * BN;
+        float *my_pb = pbuf + ew * 4 * HALF;  // [2][HALF] scaled norms, then [2][HALF] cores
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
         uint32_t tcount = 0;
         for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
@@ -438,59 +442,100 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             float L[M];
             int J[M];
 #pragma unroll
-            for (int s = 0; s < M; ++s) {
-                L[s] = CUSCAN_INF;
-                J[s] = -1;
+            for (int s2 = 0; s2 < M; ++s2) {
+                L[s2] = CUSCAN_INF;
+                J[s2] = -1;
             }
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
-            bool ok = true;
-            for (int64_t t = 0; t < P.n_tiles; ++t) {
-                if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
-                const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
-                // stage the scaled column norms of this tile for the fast test
-                float *pb = my_pbuf + b * BN;
-                {
-                    const float4 *src = reinterpret_cast<const float4 *>(P.pnorm + t * BN);
-                    float4 v0 = src[lane * 2], v1 = src[lane * 2 + 1];
-                    const float s = P.one_minus_cb;
-                    v0.x *= s; v0.y *= s; v0.z *= s; v0.w *= s;
-                    v1.x *= s; v1.y *= s; v1.z *= s; v1.w *= s;
-                    reinterpret_cast<float4 *>(pb)[lane * 2] = v0;
-                    reinterpret_cast<float4 *>(pb)[lane * 2 + 1] = v1;
+            auto next_tile = [&](int64_t t) -> int64_t {
+                while (t < P.n_tiles && tile_skipped<BORUVKA>(P, t, qlo, qhi)) ++t;
+                return t;
+            };
+            // per-tile column data, fetched one tile ahead
+            float4 pre_p = make_float4(0, 0, 0, 0), pre_c = make_float4(0, 0, 0, 0);
+            int32_t pre_ch = -2;
+            float pre_mt = 0.0f;
+            auto prefetch = [&](int64_t t) {
+                const int64_t col = t * BN + half * HALF + lane * 4;
+                pre_p = *reinterpret_cast<const float4 *>(P.pnorm + col);
+                pre_mt = P.tile_mmax[t];
+                if (BORUVKA) {
+                    // core has n entries (no padding): guard the ragged end element by element
+                    if (col + 4 <= P.n) {
+                        pre_c = *reinterpret_cast<const float4 *>(P.core + col);
+                    } else {
+                        pre_c.x = col + 0 < P.n ? P.core[col + 0] : 0.0f;
+                        pre_c.y = col + 1 < P.n ? P.core[col + 1] : 0.0f;
+                        pre_c.z = col + 2 < P.n ? P.core[col + 2] : 0.0f;
+                        pre_c.w = col + 3 < P.n ? P.core[col + 3] : 0.0f;
+                    }
+                    const int64_t ch = t * 8 + half * 4 + (lane & 3);
+                    pre_ch = -2;
+                    if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
                 }
+            };
+            int64_t t = next_tile(0);
+            if (t < P.n_tiles) prefetch(t);
+            bool ok = true;
+            while (t < P.n_tiles) {
+                const int64_t t_next = next_tile(t + 1);
+                const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
+                float *pb = my_pb + b * HALF;
+                float *cb = my_pb + (2 + b) * HALF;
+                {
+                    const float sc = P.one_minus_cb;
+                    reinterpret_cast<float4 *>(pb)[lane] =
+                        make_float4(pre_p.x * sc, pre_p.y * sc, pre_p.z * sc, pre_p.w * sc);
+                    if (BORUVKA) reinterpret_cast<float4 *>(cb)[lane] = pre_c;
+                }
+                const float mt = pre_mt;
+                const int32_t ch_word = pre_ch;
                 __syncwarp();
-                const float mt = P.tile_mmax[t];
+                if (t_next < P.n_tiles) prefetch(t_next);
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
-                const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN;
-                for (int c = 0; c < BN / 32; ++c) {
+                const uint32_t taddr =
+                    tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN + half * HALF;
+                for (int c = 0; c < HALF / 32; ++c) {
                     float v[32];
                     tmem_ld32(taddr + c * 32, v);
                     if (P.debug_tile && blockIdx.x == 0 && tcount == 0) {
 #pragma unroll
-                        for (int e = 0; e < 32; ++e) P.debug_tile[row_local * BN + c * 32 + e] = v[e];
+                        for (int e = 0; e < 32; ++e)
+                            P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
                     }
                     bool active = valid;
                     if (BORUVKA) {
-                        const int64_t ch = t * 8 + c;
-                        if (ch >= P.n_chunks) active = false;
-                        else if (P.chunk_lo[ch] == lab_i && P.chunk_hi[ch] == lab_i) active = false;
+                        const int32_t clo = __shfl_sync(0xffffffffu, ch_word, c);
+                        const int32_t chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
+                        if (clo == -2 || (clo == lab_i && chi == lab_i)) active = false;
                     }
                     // fast threshold, widened by a few ulps so that the fast test never rejects
                     // a pair whose exact-path bound would enter the list
-                    const float base = L[M - 1] - ps_i + cm_i * mt;
-                    const float thr2 = base + 0x1p-21f * (fabsf(L[M - 1]) + ps_i + cm_i * mt);
+                    const float T = L[M - 1];
+                    const float base = T - ps_i + cm_i * mt;
+                    const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
                     unsigned hits = 0;
-                    if (active) {
+                    if (active && (!BORUVKA || core_i < T)) {
                         const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
+                        const float4 *cc = reinterpret_cast<const float4 *>(cb + c * 32);
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
                             const float4 pq = pc[q];
-                            hits |= (fmaf(-2.0f, v[4 * q + 0], pq.x) < thr2) ? (1u << (4 * q + 0)) : 0u;
-                            hits |= (fmaf(-2.0f, v[4 * q + 1], pq.y) < thr2) ? (1u << (4 * q + 1)) : 0u;
-                            hits |= (fmaf(-2.0f, v[4 * q + 2], pq.z) < thr2) ? (1u << (4 * q + 2)) : 0u;
-                            hits |= (fmaf(-2.0f, v[4 * q + 3], pq.w) < thr2) ? (1u << (4 * q + 3)) : 0u;
+                            bool h0 = fmaf(-2.0f, v[4 * q + 0], pq.x) < thr2;
+                            bool h1 = fmaf(-2.0f, v[4 * q + 1], pq.y) < thr2;
+                            bool h2 = fmaf(-2.0f, v[4 * q + 2], pq.z) < thr2;
+                            bool h3 = fmaf(-2.0f, v[4 * q + 3], pq.w) < thr2;
+                            if (BORUVKA) {
+                                const float4 cq = cc[q];
+                                h0 = h0 && cq.x < T;
+                                h1 = h1 && cq.y < T;
+                                h2 = h2 && cq.z < T;
+                                h3 = h3 && cq.w < T;
+                            }
+                            hits |= (h0 ? (1u << (4 * q + 0)) : 0u) | (h1 ? (1u << (4 * q + 1)) : 0u) |
+                                    (h2 ? (1u << (4 * q + 2)) : 0u) | (h3 ? (1u << (4 * q + 3)) : 0u);
                         }
                     }
                     if (__any_sync(0xffffffffu, hits != 0u)) {
@@ -503,7 +548,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         while (hits) {
                             const int e = __ffs(hits) - 1;
                             hits &= hits - 1;
-                            const int64_t j = t * BN + c * 32 + e;
+                            const int64_t j = t * BN + half * HALF + c * 32 + e;
                             if (j >= P.n) continue;
                             if (!BORUVKA && j == row) continue;
                             const float dot = my_v[e];
@@ -524,13 +569,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&t_empty[b]);
                 ++tcount;
+                t = t_next;
             }
             if (!ok) break;
             if (valid) {
+                const int64_t base_at = row * (2 * M) + half * M;
 #pragma unroll
-                for (int s = 0; s < M; ++s) {
-                    P.cand_ids[row * M + s] = J[s];
-                    P.cand_lb[row * M + s] = L[s];
+                for (int s2 = 0; s2 < M; ++s2) {
+                    P.cand_ids[base_at + s2] = J[s2];
+                    P.cand_lb[base_at + s2] = L[s2];
                 }
             }
         }
@@ -564,7 +611,18 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
     return v;
 }
 
-// kNN re-rank: one warp per row, exact distances of the M candidates, top-k by (d, id).
+// Lower bound of every pair a row's two lists left out: a full list rejected or evicted only
+// pairs whose bound is >= its M-th entry; a list that is not full kept every pair it saw.
+template <int M>
+__device__ __forceinline__ float unseen_bound(const int32_t *ids, const float *lb) {
+    float b = CUSCAN_INF;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (ids[h * M + M - 1] >= 0) b = fminf(b, lb[h * M + M - 1]);
+    return b;
+}
+
+// kNN re-rank: one warp per row, exact distances of the 2M candidates, top-k by (d, id).
 template <int M>
 __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d, int k,
                                   const int32_t *__restrict__ cand_ids,
@@ -574,13 +632,14 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
-    constexpr int PER = M / 32;
+    constexpr int W = 2 * M;  // two lists of M per row (one per column half)
+    constexpr int PER = W / 32;
     unsigned long long key[PER];
     const float *xr = x + row * d;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const int s = q * 32 + lane;
-        const int32_t j = cand_ids[row * M + s];
+        const int32_t j = cand_ids[row * W + s];
         if (j < 0) {
             key[q] = ~0ull;
         } else {
@@ -611,10 +670,9 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
             }
         }
     }
-    // every pair outside the list has a lower bound >= the M-th bound
-    const float bound = cand_lb[row * M + M - 1];
-    const bool full = cand_ids[row * M + M - 1] >= 0;
-    if (lane == 0 && full && !(bound > dk)) {
+    // every pair outside a full list has a lower bound >= that list's M-th bound
+    const float bound = unseen_bound<M>(cand_ids + row * W, cand_lb + row * W);
+    if (lane == 0 && !(bound > dk)) {
         const int at = atomicAdd(fallback_count, 1);
         fallback[at] = (int32_t)row;
     }
@@ -634,14 +692,15 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
     const int64_t pos = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (pos >= n) return;
-    constexpr int PER = M / 32;
+    constexpr int W = 2 * M;
+    constexpr int PER = W / 32;
     const float *xr = xp + pos * d;
     const float ci = corep[pos];
     const int32_t li = labp[pos];
     unsigned long long mine = ~0ull;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
-        const int32_t j = cand_ids[pos * M + q * 32 + lane];
+        const int32_t j = cand_ids[pos * W + q * 32 + lane];
         if (j < 0 || labp[j] == li) continue;
         const float w = fmaxf(fmaxf(exact_d2(xr, xp + (int64_t)j * d, d), ci), corep[j]);
         if (w != w) continue;
@@ -651,11 +710,10 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
     }
     const unsigned long long best = warp_min_u64(mine);
     if (lane == 0) {
-        const float bound = cand_lb[pos * M + M - 1];
-        const bool full = cand_ids[pos * M + M - 1] >= 0;
+        const float bound = unseen_bound<M>(cand_ids + pos * W, cand_lb + pos * W);
         const float wmin = best == ~0ull ? CUSCAN_INF : __uint_as_float((uint32_t)(best >> 32));
         if (best != ~0ull) row_keys[perm[pos]] = best;
-        if (best == ~0ull || (full && !(bound > wmin))) {
+        if (best == ~0ull || !(bound > wmin)) {
             const int at = atomicAdd(fallback_count, 1);
             fallback[at] = (int32_t)pos;
         }
@@ -694,9 +752,9 @@ static bool refined_layout(int64_t n, int d, Layout &L) {
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
     const size_t a = (size_t)L.kblocks * KBLOCK_A, b = (size_t)L.kblocks * KBLOCK_B;
-    const size_t fixed = a + (size_t)EPI_WARPS * 2 * BN * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+    const size_t fixed = a + (size_t)EPI_WARPS * 4 * HALF * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
                          256 + 1024;
-    int st = (int)((210 * 1024 - fixed) / b);
+    int st = (int)((227 * 1024 - fixed) / b);
     if (st > 4) st = 4;
     if (st < 2) return false;
     L.stages = st;
@@ -737,8 +795,8 @@ template <int M, bool BORUVKA>
 static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64_t n, int d,
                       const float *core, const int32_t *label, const int32_t *chunk_lo,
                       const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr) {
-    int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * M, "screen candidates");
-    if (!rc) rc = ensure(ctx, R.cand_lb, sizeof(float) * n * M, "screen bounds");
+    int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * 2 * M, "screen candidates");
+    if (!rc) rc = ensure(ctx, R.cand_lb, sizeof(float) * n * 2 * M, "screen bounds");
     if (rc) return rc;
     Params P{};
     P.xt = as<uint8_t>(R.xt);
