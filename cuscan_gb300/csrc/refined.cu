@@ -276,8 +276,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     const uint32_t b_bytes = (uint32_t)P.kblocks * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
-    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][4][HALF]
-    float *vstage = pbuf + EPI_WARPS * 4 * HALF;                     // [EPI_WARPS][32][VSTRIDE]
+    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][6][HALF]
+    float *vstage = pbuf + EPI_WARPS * 6 * HALF;                     // [EPI_WARPS][32][VSTRIDE]
     uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
     uint64_t *full = bars;
     uint64_t *empty = bars + P.stages;
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         const int quad = warp & 3;            // TMEM lane quadrant of this warp
         const int half = ew >> 2;             // column half of each tile
         const int row_local = quad * 32 + lane;
-        float *my_pb = pbuf + ew * 4 * HALF;  // [2][HALF] scaled norms, then [2][HALF] cores
+        float *my_pb = pbuf + ew * 6 * HALF;  // [2][HALF] scaled norms, [2][HALF] cores, [2][HALF] m
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
         uint32_t tcount = 0;
         for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
@@ -454,11 +454,13 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             };
             // per-tile column data, fetched one tile ahead
             float4 pre_p = make_float4(0, 0, 0, 0), pre_c = make_float4(0, 0, 0, 0);
+            float4 pre_m = make_float4(0, 0, 0, 0);
             int32_t pre_ch = -2;
             float pre_mt = 0.0f;
             auto prefetch = [&](int64_t t) {
                 const int64_t col = t * BN + half * HALF + lane * 4;
                 pre_p = *reinterpret_cast<const float4 *>(P.pnorm + col);
+                pre_m = *reinterpret_cast<const float4 *>(P.mnorm + col);
                 pre_mt = P.tile_mmax[t];
                 if (BORUVKA) {
                     // core has n entries (no padding): guard the ragged end element by element
@@ -483,10 +485,12 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
                 float *cb = my_pb + (2 + b) * HALF;
+                float *mb = my_pb + (4 + b) * HALF;
                 {
                     const float sc = P.one_minus_cb;
                     reinterpret_cast<float4 *>(pb)[lane] =
                         make_float4(pre_p.x * sc, pre_p.y * sc, pre_p.z * sc, pre_p.w * sc);
+                    reinterpret_cast<float4 *>(mb)[lane] = pre_m;
                     if (BORUVKA) reinterpret_cast<float4 *>(cb)[lane] = pre_c;
                 }
                 const float mt = pre_mt;
@@ -506,59 +510,88 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
                     }
                     bool active = valid;
+                    int32_t clo = 0, chi = 0;
                     if (BORUVKA) {
-                        const int32_t clo = __shfl_sync(0xffffffffu, ch_word, c);
-                        const int32_t chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
+                        clo = __shfl_sync(0xffffffffu, ch_word, c);
+                        chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
                         if (clo == -2 || (clo == lab_i && chi == lab_i)) active = false;
                     }
-                    // fast threshold, widened by a few ulps so that the fast test never rejects
-                    // a pair whose exact-path bound would enter the list
+                    // Fast test on the running minimum of the chunk. thr2 is the list threshold
+                    // moved to the scale of F = (1 - C_B) p_j - 2 dot with the tile's largest
+                    // norm, then widened by a few ulps so that no pair whose exact-path bound
+                    // would enter the list is passed over. For Borůvka the core condition
+                    // core_j < T rides along as max(F, core_j + (thr2 - T)).
                     const float T = L[M - 1];
                     const float base = T - ps_i + cm_i * mt;
                     const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
-                    unsigned hits = 0;
+                    const float dlt = thr2 - T;
+                    const float thr_fast = thr2 + 0x1p-20f * (fabsf(thr2) + fabsf(T));
+                    float mn = CUSCAN_INF;
                     if (active && (!BORUVKA || core_i < T)) {
                         const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
                         const float4 *cc = reinterpret_cast<const float4 *>(cb + c * 32);
 #pragma unroll
                         for (int q = 0; q < 8; ++q) {
                             const float4 pq = pc[q];
-                            bool h0 = fmaf(-2.0f, v[4 * q + 0], pq.x) < thr2;
-                            bool h1 = fmaf(-2.0f, v[4 * q + 1], pq.y) < thr2;
-                            bool h2 = fmaf(-2.0f, v[4 * q + 2], pq.z) < thr2;
-                            bool h3 = fmaf(-2.0f, v[4 * q + 3], pq.w) < thr2;
+                            float f0 = fmaf(-2.0f, v[4 * q + 0], pq.x);
+                            float f1 = fmaf(-2.0f, v[4 * q + 1], pq.y);
+                            float f2 = fmaf(-2.0f, v[4 * q + 2], pq.z);
+                            float f3 = fmaf(-2.0f, v[4 * q + 3], pq.w);
                             if (BORUVKA) {
                                 const float4 cq = cc[q];
-                                h0 = h0 && cq.x < T;
-                                h1 = h1 && cq.y < T;
-                                h2 = h2 && cq.z < T;
-                                h3 = h3 && cq.w < T;
+                                f0 = fmaxf(f0, cq.x + dlt);
+                                f1 = fmaxf(f1, cq.y + dlt);
+                                f2 = fmaxf(f2, cq.z + dlt);
+                                f3 = fmaxf(f3, cq.w + dlt);
                             }
-                            hits |= (h0 ? (1u << (4 * q + 0)) : 0u) | (h1 ? (1u << (4 * q + 1)) : 0u) |
-                                    (h2 ? (1u << (4 * q + 2)) : 0u) | (h3 ? (1u << (4 * q + 3)) : 0u);
+                            mn = fminf(mn, fminf(fminf(f0, f1), fminf(f2, f3)));
                         }
                     }
-                    if (__any_sync(0xffffffffu, hits != 0u)) {
-                        if (hits) {
+                    const bool any_hit = mn < thr_fast;
+                    if (__any_sync(0xffffffffu, any_hit)) {
+                        unsigned hits = 0;
+                        if (any_hit) {
+                            const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
+                            const float4 *cc = reinterpret_cast<const float4 *>(cb + c * 32);
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const float4 pq = pc[q];
+                                float f0 = fmaf(-2.0f, v[4 * q + 0], pq.x);
+                                float f1 = fmaf(-2.0f, v[4 * q + 1], pq.y);
+                                float f2 = fmaf(-2.0f, v[4 * q + 2], pq.z);
+                                float f3 = fmaf(-2.0f, v[4 * q + 3], pq.w);
+                                if (BORUVKA) {
+                                    const float4 cq = cc[q];
+                                    f0 = fmaxf(f0, cq.x + dlt);
+                                    f1 = fmaxf(f1, cq.y + dlt);
+                                    f2 = fmaxf(f2, cq.z + dlt);
+                                    f3 = fmaxf(f3, cq.w + dlt);
+                                }
+                                hits |= (f0 < thr_fast ? 1u : 0u) << (4 * q + 0);
+                                hits |= (f1 < thr_fast ? 1u : 0u) << (4 * q + 1);
+                                hits |= (f2 < thr_fast ? 1u : 0u) << (4 * q + 2);
+                                hits |= (f3 < thr_fast ? 1u : 0u) << (4 * q + 3);
+                            }
 #pragma unroll
                             for (int q = 0; q < 8; ++q)
                                 reinterpret_cast<float4 *>(my_v)[q] =
                                     make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                         }
+                        const bool uniform_other = BORUVKA && clo == chi && clo != lab_i;
                         while (hits) {
                             const int e = __ffs(hits) - 1;
                             hits &= hits - 1;
-                            const int64_t j = t * BN + half * HALF + c * 32 + e;
+                            const int col = c * 32 + e;
+                            const int64_t j = t * BN + half * HALF + col;
                             if (j >= P.n) continue;
                             if (!BORUVKA && j == row) continue;
                             const float dot = my_v[e];
                             // exact lower bound for this pair (per-column norm instead of the
-                            // tile maximum)
-                            const float pj = P.pnorm[j], mj = P.mnorm[j];
-                            float lb = fmaf(-cm_i, mj, fmaf(-2.0f, dot, P.one_minus_cb * pj) + ps_i);
+                            // tile maximum); pb holds (1 - C_B) p_j
+                            float lb = fmaf(-cm_i, mb[col], fmaf(-2.0f, dot, pb[col]) + ps_i);
                             if (BORUVKA) {
-                                if (P.label[j] == lab_i) continue;
-                                lb = fmaxf(fmaxf(lb, core_i), P.core[j]);
+                                if (!uniform_other && P.label[j] == lab_i) continue;
+                                lb = fmaxf(fmaxf(lb, core_i), cb[col]);
                             }
                             if (lb < L[M - 1]) list_insert<M>(L, J, lb, (int)j);
                         }
@@ -752,7 +785,7 @@ static bool refined_layout(int64_t n, int d, Layout &L) {
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
     const size_t a = (size_t)L.kblocks * KBLOCK_A, b = (size_t)L.kblocks * KBLOCK_B;
-    const size_t fixed = a + (size_t)EPI_WARPS * 4 * HALF * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+    const size_t fixed = a + (size_t)EPI_WARPS * 6 * HALF * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
                          256 + 1024;
     int st = (int)((227 * 1024 - fixed) / b);
     if (st > 4) st = 4;
