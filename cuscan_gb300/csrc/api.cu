@@ -252,7 +252,8 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
                                         as<int32_t>(b.tile_lo), as<int32_t>(b.tile_hi), s);
         if (rc) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[5], s));
-        if ((rc = forest_round(ctx, b, n, components, label, mst_src, mst_dst, mst_wsq, s)))
+        if ((rc = forest_round(ctx, b, n, components, label, mst_src, mst_dst, mst_wsq, s,
+                               precision == CUSCAN_PRECISION_BF16_REFINED)))
             return rc;
         if ((rc = read_status(ctx, b.status, hs, s))) return rc;
         cand_ms += elapsed(ev[4], ev[5]);

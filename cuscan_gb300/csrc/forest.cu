@@ -232,7 +232,7 @@ __global__ void component_min_kernel(const int32_t *__restrict__ perm,
                                      const int32_t *__restrict__ labp,
                                      const unsigned long long *__restrict__ row_keys, int64_t n,
                                      unsigned long long *__restrict__ comp_keys,
-                                     DevStatus *status) {
+                                     DevStatus *status, int allow_empty) {
     int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     int32_t l = -1;
@@ -242,7 +242,7 @@ __global__ void component_min_kernel(const int32_t *__restrict__ perm,
         l = labp[pos];
         unsigned long long rk = row_keys[i];
         if (rk == ~0ull) {
-            atomicCAS(&status->err_kind, 0, 4);
+            if (!allow_empty) atomicCAS(&status->err_kind, 0, 4);
         } else {
             uint32_t wb = (uint32_t)(rk >> 32);
             if (numerical_bits(wb)) {
@@ -467,13 +467,13 @@ int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, 
 
 int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t components,
                  int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
-                 cudaStream_t s) {
+                 cudaStream_t s, int allow_empty) {
     unsigned long long *comp_keys = as<unsigned long long>(b.comp_keys);
     int rc = launch_fill_u64(ctx, comp_keys, n, ~0ull, s);
     if (rc) return rc;
-    CUSCAN_KERNEL(component_min_kernel, blocks(n), 256, 0, s, as<int32_t>(b.perm), as<int32_t>(b.labp),
-                                                   as<unsigned long long>(b.row_keys), n,
-                                                   comp_keys, b.status);
+    CUSCAN_KERNEL(component_min_kernel, blocks(n), 256, 0, s, as<int32_t>(b.perm),
+                  as<int32_t>(b.labp), as<unsigned long long>(b.row_keys), n, comp_keys, b.status,
+                  allow_empty);
     CUSCAN_KERNEL(winner_kernel, blocks(n), 256, 0, s, label, comp_keys, as<unsigned long long>(b.row_keys),
                                              n, as<int32_t>(b.next), as<uint32_t>(b.esrc),
                                              as<uint32_t>(b.edst), as<float>(b.ew), b.status);
@@ -525,7 +525,8 @@ void forest_release(ForestBuffers &b) {
     for (Buffer *p : all) release(*p);
     RefinedBuffers &r = b.refined;
     Buffer *rall[] = {&r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo, &r.tile_hi,
-                      &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error};
+                      &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
+                      &r.cbound, &r.rowcnt};
     for (Buffer *p : rall) release(*p);
     b.status = nullptr;
 }

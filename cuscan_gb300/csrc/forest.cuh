@@ -17,7 +17,7 @@ struct DevStatus {
 // Buffers of the bf16 screening path (refined.cu).
 struct RefinedBuffers {
     Buffer xt, pnorm, mnorm, tile_mmax, tile_lo, tile_hi, cand_ids, cand_lb, fallback, count;
-    Buffer error;
+    Buffer error, cbound, rowcnt;
 };
 
 struct ForestBuffers {
@@ -47,9 +47,11 @@ int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int3
 int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, const float *core,
                              const int32_t *label, int64_t n, int d, cudaStream_t s);
 // Merge one round from the per-row candidate keys in b.row_keys.
+// allow_empty: rows may lack a candidate (the bf16 screen appends only pairs that can reach
+// their component's cheapest edge).
 int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t components,
                  int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
-                 cudaStream_t s);
+                 cudaStream_t s, int allow_empty = 0);
 int scan_exclusive(cuscan_ctx *ctx, const int32_t *in, int32_t *out, int64_t n,
                    int32_t *grand_total, Buffer &tmp, cudaStream_t s);
 

@@ -38,6 +38,7 @@ constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of 
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded mbarrier waits: 2 s of wall time
 constexpr uint32_t WAIT_POLLS = 1u << 22;      // poll bound of the abort-path drains
 constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
+constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row half
 
 struct Params {
     const uint8_t *xt;        // bf16 tiles, pre-swizzled (see tile_bf16_kernel)
@@ -57,6 +58,10 @@ struct Params {
     float *cand_lb;           // [n][M]
     int *error;
     float *debug_tile;        // when set: CTA 0 writes its first raw 128 x 256 accumulator tile
+    float c_b;                // norm coefficient of the bound (upper bounds use it)
+    uint32_t *cbound;         // Borůvka: per-component upper bound of the cheapest edge (f32 bits)
+    int32_t *rowcnt;          // Borůvka: candidates appended per row half ([n][2])
+    int cap;                  // Borůvka: candidate slots per row half
 };
 
 // ---- PTX wrappers ----
@@ -439,13 +444,19 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 core_i = P.core[row];
                 lab_i = P.label[row];
             }
-            float L[M];
-            int J[M];
+            // kNN: the row's M smallest lower bounds. Borůvka: an upper bound U on the row's
+            // cheapest cross-component edge plus the shared bound of its component; pairs whose
+            // lower bound does not exceed min(U, component bound) are appended for re-ranking.
+            constexpr int LM = BORUVKA ? 1 : M;
+            float L[LM];
+            int J[LM];
 #pragma unroll
-            for (int s2 = 0; s2 < M; ++s2) {
+            for (int s2 = 0; s2 < LM; ++s2) {
                 L[s2] = CUSCAN_INF;
                 J[s2] = -1;
             }
+            float U = CUSCAN_INF, published = CUSCAN_INF;
+            int cnt = 0;
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
             auto next_tile = [&](int64_t t) -> int64_t {
@@ -456,7 +467,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             float4 pre_p = make_float4(0, 0, 0, 0), pre_c = make_float4(0, 0, 0, 0);
             float4 pre_m = make_float4(0, 0, 0, 0);
             int32_t pre_ch = -2;
-            float pre_mt = 0.0f;
+            float pre_mt = 0.0f, pre_cb = CUSCAN_INF;
             auto prefetch = [&](int64_t t) {
                 const int64_t col = t * BN + half * HALF + lane * 4;
                 pre_p = *reinterpret_cast<const float4 *>(P.pnorm + col);
@@ -475,6 +486,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     const int64_t ch = t * 8 + half * 4 + (lane & 3);
                     pre_ch = -2;
                     if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
+                    pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i]) : CUSCAN_INF;
                 }
             };
             int64_t t = next_tile(0);
@@ -495,6 +507,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
                 const float mt = pre_mt;
                 const int32_t ch_word = pre_ch;
+                const float comp_bound = pre_cb;
                 __syncwarp();
                 if (t_next < P.n_tiles) prefetch(t_next);
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
@@ -521,13 +534,13 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     // norm, then widened by a few ulps so that no pair whose exact-path bound
                     // would enter the list is passed over. For Borůvka the core condition
                     // core_j < T rides along as max(F, core_j + (thr2 - T)).
-                    const float T = L[M - 1];
+                    const float T = BORUVKA ? fminf(U, comp_bound) : L[LM - 1];
                     const float base = T - ps_i + cm_i * mt;
                     const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
                     const float dlt = thr2 - T;
                     const float thr_fast = thr2 + 0x1p-20f * (fabsf(thr2) + fabsf(T));
                     float mn = CUSCAN_INF;
-                    if (active && (!BORUVKA || core_i < T)) {
+                    if (active && (!BORUVKA || core_i <= T)) {
                         const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
                         const float4 *cc = reinterpret_cast<const float4 *>(cb + c * 32);
 #pragma unroll
@@ -589,11 +602,23 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             // exact lower bound for this pair (per-column norm instead of the
                             // tile maximum); pb holds (1 - C_B) p_j
                             float lb = fmaf(-cm_i, mb[col], fmaf(-2.0f, dot, pb[col]) + ps_i);
-                            if (BORUVKA) {
+                            if constexpr (BORUVKA) {
                                 if (!uniform_other && P.label[j] == lab_i) continue;
-                                lb = fmaxf(fmaxf(lb, core_i), cb[col]);
+                                const float cj = cb[col];
+                                const float lbw = fmaxf(fmaxf(lb, core_i), cj);
+                                const float Tn = fminf(U, comp_bound);
+                                if (lbw <= Tn) {
+                                    if (cnt < P.cap) P.cand_ids[(row * 2 + half) * P.cap + cnt] = (int32_t)j;
+                                    ++cnt;
+                                    // upper bound of this pair's weight: D + eps = L + 2 eps
+                                    const float eps2 = 2.0f * fmaf(cm_i, mb[col], P.c_b * (ps_i + pb[col]) * 1.001f);
+                                    const float ubr = lb + eps2;
+                                    const float ub = fmaxf(fmaxf(ubr + 0x1p-20f * (fabsf(ubr) + eps2), core_i), cj);
+                                    U = fminf(U, ub);
+                                }
+                            } else {
+                                if (lb < L[LM - 1]) list_insert<LM>(L, J, lb, (int)j);
                             }
-                            if (lb < L[M - 1]) list_insert<M>(L, J, lb, (int)j);
                         }
                         __syncwarp();
                     }
@@ -601,14 +626,21 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&t_empty[b]);
+                if (BORUVKA && valid && U < published) {
+                    atomicMin(&P.cbound[lab_i], __float_as_uint(U));
+                    published = U;
+                }
                 ++tcount;
                 t = t_next;
             }
             if (!ok) break;
-            if (valid) {
+            if (BORUVKA) {
+                // each half of a row appends into its own slot range [(2 row + half) * cap, +cap)
+                if (valid) P.rowcnt[row * 2 + half] = cnt;
+            } else if (valid) {
                 const int64_t base_at = row * (2 * M) + half * M;
 #pragma unroll
-                for (int s2 = 0; s2 < M; ++s2) {
+                for (int s2 = 0; s2 < LM; ++s2) {
                     P.cand_ids[base_at + s2] = J[s2];
                     P.cand_lb[base_at + s2] = L[s2];
                 }
@@ -711,30 +743,37 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
     }
 }
 
-// Borůvka re-rank over component-sorted positions: exact weight of each candidate, row minimum
-// (w, original j) into row_keys[original row].
-template <int M>
+// Borůvka re-rank over component-sorted positions: exact weight of every appended candidate of
+// both row halves, row minimum (w, original j) into row_keys[original row]. Rows whose buffer
+// overflowed are re-run exactly; rows without candidates keep an empty key (they cannot hold
+// their component's cheapest edge: every pair reaching it is appended).
 __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float *__restrict__ corep,
                                       const int32_t *__restrict__ labp,
                                       const int32_t *__restrict__ perm, int64_t n, int d,
                                       const int32_t *__restrict__ cand_ids,
-                                      const float *__restrict__ cand_lb,
+                                      const int32_t *__restrict__ rowcnt, int cap,
                                       unsigned long long *__restrict__ row_keys,
                                       int32_t *__restrict__ fallback,
                                       int *__restrict__ fallback_count) {
     const int64_t pos = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (pos >= n) return;
-    constexpr int W = 2 * M;
-    constexpr int PER = W / 32;
+    const int c0 = rowcnt[pos * 2], c1 = rowcnt[pos * 2 + 1];
+    if (c0 > cap || c1 > cap) {
+        if (lane == 0) {
+            const int at = atomicAdd(fallback_count, 1);
+            fallback[at] = (int32_t)pos;
+        }
+        return;
+    }
     const float *xr = xp + pos * d;
     const float ci = corep[pos];
     const int32_t li = labp[pos];
     unsigned long long mine = ~0ull;
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int32_t j = cand_ids[pos * W + q * 32 + lane];
-        if (j < 0 || labp[j] == li) continue;
+    for (int s = lane; s < c0 + c1; s += 32) {
+        const int32_t j = s < c0 ? cand_ids[(pos * 2) * cap + s]
+                                 : cand_ids[(pos * 2 + 1) * cap + (s - c0)];
+        if (labp[j] == li) continue;
         const float w = fmaxf(fmaxf(exact_d2(xr, xp + (int64_t)j * d, d), ci), corep[j]);
         if (w != w) continue;
         const unsigned long long key =
@@ -742,15 +781,12 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
         mine = key < mine ? key : mine;
     }
     const unsigned long long best = warp_min_u64(mine);
-    if (lane == 0) {
-        const float bound = unseen_bound<M>(cand_ids + pos * W, cand_lb + pos * W);
-        const float wmin = best == ~0ull ? CUSCAN_INF : __uint_as_float((uint32_t)(best >> 32));
-        if (best != ~0ull) row_keys[perm[pos]] = best;
-        if (best == ~0ull || !(bound > wmin)) {
-            const int at = atomicAdd(fallback_count, 1);
-            fallback[at] = (int32_t)pos;
-        }
-    }
+    if (lane == 0 && best != ~0ull) row_keys[perm[pos]] = best;
+}
+
+__global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
 }
 
 // Error bound coefficients for d features (K = padded depth of the bf16 dot product).
@@ -856,6 +892,18 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.cand_lb = as<float>(R.cand_lb);
     P.error = as<int>(R.error);
     P.debug_tile = debug_tile;
+    P.c_b = cb;
+    P.cap = BORUVKA_CAP;
+    if (BORUVKA) {
+        rc = ensure(ctx, R.cbound, sizeof(uint32_t) * n, "component bounds");
+        if (!rc) rc = ensure(ctx, R.rowcnt, sizeof(int32_t) * 2 * n, "row candidate counts");
+        if (rc) return rc;
+        P.cbound = as<uint32_t>(R.cbound);
+        P.rowcnt = as<int32_t>(R.rowcnt);
+        CUSCAN_KERNEL(fill_u32_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, P.cbound, n,
+                      0x7f800000u);
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowcnt.ptr, 0, sizeof(int32_t) * 2 * n, s));
+    }
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
     auto kernel = screen_kernel<M, BORUVKA>;
     CUSCAN_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -927,9 +975,9 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     constexpr int M = 32;
     if ((rc = run_screen<M, true>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    CUSCAN_KERNEL(rerank_boruvka_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xp, corep,
-                  labp, perm, n, d, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), row_keys,
-                  as<int32_t>(R.fallback), as<int>(R.count));
+    CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xp, corep,
+                  labp, perm, n, d, as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
+                  row_keys, as<int32_t>(R.fallback), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
     int fallbacks = 0;
     if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
