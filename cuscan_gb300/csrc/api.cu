@@ -22,7 +22,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
                        int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
                        int64_t *fallback_rows);
 int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
-                              cudaStream_t s, int64_t *fallback_rows);
+                              const int32_t *knn_ids, const float *knn_sq, int k,
+                              const float *core, const int32_t *label, cudaStream_t s,
+                              int64_t *fallback_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
                       float *out, cudaStream_t s);
 
@@ -245,7 +247,8 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if ((rc = launch_fill_u64(ctx, row_keys, n, ~0ull, s))) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[4], s));
         if (precision == CUSCAN_PRECISION_BF16_REFINED)
-            rc = launch_candidates_refined(ctx, b, n, d, s, &boruvka_fallback_rows);
+            rc = launch_candidates_refined(ctx, b, n, d, knn_ids, knn_sq, k, core_sq, label, s,
+                                           &boruvka_fallback_rows);
         else
             rc = launch_candidates_fp32(ctx, as<float>(b.xp), as<float>(b.corep),
                                         as<int32_t>(b.labp), as<int32_t>(b.perm), n, d, row_keys,

@@ -221,7 +221,7 @@ __global__ void gather_kernel(const float *__restrict__ x, const float *__restri
     int32_t i = perm[pos];
     xp[e] = x[(int64_t)i * d + f];
     if (f == 0) {
-        corep[pos] = core[i];
+        if (core) corep[pos] = core[i];
         labp[pos] = label[i];
     }
 }
@@ -526,7 +526,7 @@ void forest_release(ForestBuffers &b) {
     RefinedBuffers &r = b.refined;
     Buffer *rall[] = {&r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo, &r.tile_hi,
                       &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
-                      &r.cbound, &r.rowcnt};
+                      &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d};
     for (Buffer *p : rall) release(*p);
     b.status = nullptr;
 }

@@ -17,7 +17,7 @@ struct DevStatus {
 // Buffers of the bf16 screening path (refined.cu).
 struct RefinedBuffers {
     Buffer xt, pnorm, mnorm, tile_mmax, tile_lo, tile_hi, cand_ids, cand_lb, fallback, count;
-    Buffer error, cbound, rowcnt;
+    Buffer error, cbound, rowcnt, pivots, cells, cell_d;
 };
 
 struct ForestBuffers {

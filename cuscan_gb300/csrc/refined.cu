@@ -238,6 +238,14 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
     }
 }
 
+// Order in which query block qb visits the reference tiles: starting with the tile that holds
+// the block itself and wrapping around. In cell-sorted data the first tiles hold the block's
+// nearest neighbours, so the per-row thresholds tighten early and later tiles rarely hit.
+__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t qb, int64_t i) {
+    int64_t t = (qb * BM) / BN + i;
+    return t >= P.n_tiles ? t - P.n_tiles : t;
+}
+
 // Label range of query block qb (4 chunks of 32 rows).
 __device__ __forceinline__ void qblock_range(const Params &P, int64_t qb, int32_t &lo,
                                              int32_t &hi) {
@@ -341,7 +349,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     bulk_g2s(sA + kb * KBLOCK_A, asrc + (uint64_t)kb * KBLOCK_B, KBLOCK_A, a_full);
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
-                for (int64_t t = 0; t < P.n_tiles; ++t) {
+                for (int64_t i = 0; i < P.n_tiles; ++i) {
+                    const int64_t t = tile_order(P, qb, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
                     issued[stage] = 2u | phase;
@@ -383,7 +392,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 bool ok = true;
-                for (int64_t t = 0; t < P.n_tiles; ++t) {
+                for (int64_t i = 0; i < P.n_tiles; ++i) {
+                    const int64_t t = tile_order(P, qb, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                     if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
@@ -459,9 +469,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             int cnt = 0;
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
-            auto next_tile = [&](int64_t t) -> int64_t {
-                while (t < P.n_tiles && tile_skipped<BORUVKA>(P, t, qlo, qhi)) ++t;
-                return t;
+            // next visited position i (>= i0) in this block's tile order
+            auto next_index = [&](int64_t i) -> int64_t {
+                while (i < P.n_tiles && tile_skipped<BORUVKA>(P, tile_order(P, qb, i), qlo, qhi)) ++i;
+                return i;
             };
             // per-tile column data, fetched one tile ahead
             float4 pre_p = make_float4(0, 0, 0, 0), pre_c = make_float4(0, 0, 0, 0);
@@ -489,11 +500,12 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i]) : CUSCAN_INF;
                 }
             };
-            int64_t t = next_tile(0);
-            if (t < P.n_tiles) prefetch(t);
+            int64_t ti = next_index(0);
+            if (ti < P.n_tiles) prefetch(tile_order(P, qb, ti));
             bool ok = true;
-            while (t < P.n_tiles) {
-                const int64_t t_next = next_tile(t + 1);
+            while (ti < P.n_tiles) {
+                const int64_t t = tile_order(P, qb, ti);
+                const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
                 float *cb = my_pb + (2 + b) * HALF;
@@ -509,7 +521,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb;
                 __syncwarp();
-                if (t_next < P.n_tiles) prefetch(t_next);
+                if (ti_next < P.n_tiles) prefetch(tile_order(P, qb, ti_next));
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -631,7 +643,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     published = U;
                 }
                 ++tcount;
-                t = t_next;
+                ti = ti_next;
             }
             if (!ok) break;
             if (BORUVKA) {
@@ -688,9 +700,11 @@ __device__ __forceinline__ float unseen_bound(const int32_t *ids, const float *l
 }
 
 // kNN re-rank: one warp per row, exact distances of the 2M candidates, top-k by (d, id).
+// x and the candidates are in sorted positions; perm maps a position to its original row, which
+// is the id the reference orders ties by and the row the output goes to.
 template <int M>
-__global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d, int k,
-                                  const int32_t *__restrict__ cand_ids,
+__global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__restrict__ perm,
+                                  int64_t n, int d, int k, const int32_t *__restrict__ cand_ids,
                                   const float *__restrict__ cand_lb, int32_t *__restrict__ ids,
                                   float *__restrict__ dist, int32_t *__restrict__ fallback,
                                   int *__restrict__ fallback_count) {
@@ -709,9 +723,10 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
             key[q] = ~0ull;
         } else {
             const float dd = exact_d2(xr, x + (int64_t)j * d, d);
-            key[q] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)j;
+            key[q] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
         }
     }
+    const int64_t orow = perm[row];
     float dk = CUSCAN_INF;
     for (int r = 0; r < k; ++r) {
         unsigned long long mine = key[0];
@@ -723,15 +738,15 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
             if (key[q] == best) key[q] = ~0ull;
         if (best == ~0ull) {
             if (lane == 0) {
-                ids[row * k + r] = (int32_t)n;
-                dist[row * k + r] = CUSCAN_INF;
+                ids[orow * k + r] = (int32_t)n;
+                dist[orow * k + r] = CUSCAN_INF;
             }
             dk = CUSCAN_INF;
         } else {
             dk = __uint_as_float((uint32_t)(best >> 32));
             if (lane == 0) {
-                ids[row * k + r] = (int32_t)(uint32_t)best;
-                dist[row * k + r] = dk;
+                ids[orow * k + r] = (int32_t)(uint32_t)best;
+                dist[orow * k + r] = dk;
             }
         }
     }
@@ -739,7 +754,7 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, int64_t n, int d,
     const float bound = unseen_bound<M>(cand_ids + row * W, cand_lb + row * W);
     if (lane == 0 && !(bound > dk)) {
         const int at = atomicAdd(fallback_count, 1);
-        fallback[at] = (int32_t)row;
+        fallback[at] = (int32_t)orow;
     }
 }
 
@@ -782,6 +797,36 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
     }
     const unsigned long long best = warp_min_u64(mine);
     if (lane == 0 && best != ~0ull) row_keys[perm[pos]] = best;
+}
+
+// Upper bounds of each component's cheapest edge from the exact kNN rows: a neighbour in another
+// component is an edge of known exact weight max(d2, core_i, core_j).
+__global__ void seed_bounds_kernel(const int32_t *__restrict__ knn_ids,
+                                   const float *__restrict__ knn_sq, int k,
+                                   const float *__restrict__ core, const int32_t *__restrict__ label,
+                                   int64_t n, uint32_t *__restrict__ cbound) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t li = label[i];
+    const float ci = core[i];
+    float best = CUSCAN_INF;
+    for (int s = 0; s < k; ++s) {
+        const int32_t j = knn_ids[i * k + s];
+        if (j < 0 || (int64_t)j >= n || label[j] == li) continue;
+        best = fminf(best, fmaxf(fmaxf(knn_sq[i * k + s], ci), core[j]));
+    }
+    if (best < CUSCAN_INF) atomicMin(&cbound[li], __float_as_uint(best));
+}
+
+// Evenly spaced rows as cell pivots.
+__global__ void pick_pivots_kernel(const float *__restrict__ x, int64_t n, int d, int npiv,
+                                   float *__restrict__ piv) {
+    int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)npiv * d) return;
+    const int64_t p = e / d;
+    const int f = (int)(e - p * d);
+    const int64_t r = (p * n) / npiv;
+    piv[e] = x[r * d + f];
 }
 
 __global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
@@ -900,8 +945,6 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         if (rc) return rc;
         P.cbound = as<uint32_t>(R.cbound);
         P.rowcnt = as<int32_t>(R.rowcnt);
-        CUSCAN_KERNEL(fill_u32_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, P.cbound, n,
-                      0x7f800000u);
         CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowcnt.ptr, 0, sizeof(int32_t) * 2 * n, s));
     }
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
@@ -937,19 +980,38 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     RefinedBuffers &R = b.refined;
     Layout L;
     refined_layout(n, d, L);
-    int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
+    // 1. cells: nearest of npiv evenly spaced pivot rows (exact f32, k = 1)
+    const int npiv = (int)(n / 256 < 256 ? (n / 256 < 1 ? 1 : n / 256) : 256);
+    int rc = ensure(ctx, R.pivots, sizeof(float) * npiv * d, "cell pivots");
+    if (!rc) rc = ensure(ctx, R.cells, sizeof(int32_t) * n, "cells");
+    if (!rc) rc = ensure(ctx, R.cell_d, sizeof(float) * n, "cell distances");
     if (rc) return rc;
+    CUSCAN_KERNEL(pick_pivots_kernel, (unsigned)ceil_div((int64_t)npiv * d, 256), 256, 0, s, x, n,
+                  d, npiv, as<float>(R.pivots));
+    CUSCAN_LAUNCH(ctx, "pick_pivots_kernel");
+    if ((rc = launch_exact_knn_fp32(ctx, x, n, as<float>(R.pivots), npiv, d, 1, 0, 0, 1,
+                                    as<int32_t>(R.cells), as<float>(R.cell_d), s, b.knn_ids_tmp,
+                                    b.knn_dist_tmp)))
+        return rc;
+    // 2. rows sorted by cell (b.perm, b.xp)
+    if ((rc = forest_sort_by_component(ctx, b, x, nullptr, as<int32_t>(R.cells), n, d, s)))
+        return rc;
+    const float *xs = as<float>(b.xp);
+    const int32_t *perm = as<int32_t>(b.perm);
+    // 3. screen + exact re-rank in sorted positions, outputs in original rows
+    if ((rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s))) return rc;
     constexpr int M = 32;
     if ((rc = run_screen<M, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, x, n, d, k,
-                  as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
+    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xs, perm, n, d,
+                  k, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
                   as<int32_t>(R.fallback), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
     int fallbacks = 0;
     if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
     if (refined_rows) *refined_rows += n;
     if (fallback_rows) *fallback_rows += fallbacks;
+    // 4. inconclusive rows (original indices): exact f32 sweep
     if (fallbacks > 0)
         return launch_exact_knn_fp32(ctx, x, fallbacks, x, n, d, k, 1, 0, 1, ids, dist, s,
                                      b.knn_ids_tmp, b.knn_dist_tmp, as<int32_t>(R.fallback));
@@ -957,7 +1019,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
 }
 
 int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
-                              cudaStream_t s, int64_t *fallback_rows) {
+                              const int32_t *knn_ids, const float *knn_sq, int k,
+                              const float *core, const int32_t *label, cudaStream_t s,
+                              int64_t *fallback_rows) {
     const float *xp = as<float>(b.xp);
     const float *corep = as<float>(b.corep);
     const int32_t *labp = as<int32_t>(b.labp);
@@ -972,6 +1036,13 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     int rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
     if (!rc) rc = prep(ctx, R, L, xp, n, d, clo, chi, s);
     if (rc) return rc;
+    // component bounds: +inf, then the exact cross-component edges of the kNN rows
+    if ((rc = ensure(ctx, R.cbound, sizeof(uint32_t) * n, "component bounds"))) return rc;
+    CUSCAN_KERNEL(fill_u32_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, as<uint32_t>(R.cbound), n,
+                  0x7f800000u);
+    CUSCAN_KERNEL(seed_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, knn_ids, knn_sq, k,
+                  core, label, n, as<uint32_t>(R.cbound));
+    CUSCAN_LAUNCH(ctx, "component bounds");
     constexpr int M = 32;
     if ((rc = run_screen<M, true>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
