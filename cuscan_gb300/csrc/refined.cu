@@ -151,8 +151,8 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
             smem_u32(bar))
         : "memory");
 }
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// Issue a 32-column TMEM load (no wait): the registers are valid only after tmem_ld_wait.
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
         "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -163,9 +163,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
           "=r"(r[31])
         : "r"(taddr));
+}
+// Wait for every issued TMEM load; the register operands tie r to the wait so the compiler
+// cannot read them earlier.
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+    asm volatile(""
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                   "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                   "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]),
+                   "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]),
+                   "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
 }
 
 // Byte offset of element (row r, feature f) in the tiled bf16 copy: 256-row tiles, each split
@@ -526,9 +535,30 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 const uint32_t taddr =
                     tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN + half * HALF;
+                // TMEM loads are software pipelined: chunk c+1 is in flight while chunk c is
+                // screened (rA/rB alternate; the loop is unrolled so both stay in registers)
+                // (Borůvka only: the kNN list leaves no room for the second buffer)
+                constexpr bool PIPE = BORUVKA;
+                uint32_t rA[32], rB[PIPE ? 32 : 1];
+                tmem_ld32_issue(taddr, rA);
+                tmem_ld_wait(rA);
+#pragma unroll
                 for (int c = 0; c < HALF / 32; ++c) {
+                    uint32_t(&rc_)[32] = rA;
+                    if constexpr (PIPE) {
+                        if (c > 0) {
+                            // the chunk loaded into rB during the previous step becomes current
+#pragma unroll
+                            for (int e = 0; e < 32; ++e) rA[e] = rB[e];
+                        }
+                        if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
+                    } else if (c > 0) {
+                        tmem_ld32_issue(taddr + c * 32, rA);
+                        tmem_ld_wait(rA);
+                    }
                     float v[32];
-                    tmem_ld32(taddr + c * 32, v);
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(rc_[e]);
                     if (P.debug_tile && blockIdx.x == 0 && tcount == 0) {
 #pragma unroll
                         for (int e = 0; e < 32; ++e)
@@ -562,13 +592,6 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             float f1 = fmaf(-2.0f, v[4 * q + 1], pq.y);
                             float f2 = fmaf(-2.0f, v[4 * q + 2], pq.z);
                             float f3 = fmaf(-2.0f, v[4 * q + 3], pq.w);
-                            if (BORUVKA) {
-                                const float4 cq = cc[q];
-                                f0 = fmaxf(f0, cq.x + dlt);
-                                f1 = fmaxf(f1, cq.y + dlt);
-                                f2 = fmaxf(f2, cq.z + dlt);
-                                f3 = fmaxf(f3, cq.w + dlt);
-                            }
                             mn = fminf(mn, fminf(fminf(f0, f1), fminf(f2, f3)));
                         }
                     }
@@ -586,6 +609,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                                 float f2 = fmaf(-2.0f, v[4 * q + 2], pq.z);
                                 float f3 = fmaf(-2.0f, v[4 * q + 3], pq.w);
                                 if (BORUVKA) {
+                                    // core_j <= T is necessary for an append
                                     const float4 cq = cc[q];
                                     f0 = fmaxf(f0, cq.x + dlt);
                                     f1 = fmaxf(f1, cq.y + dlt);
@@ -633,6 +657,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             }
                         }
                         __syncwarp();
+                    }
+                    if constexpr (PIPE) {
+                        if (c + 1 < HALF / 32) tmem_ld_wait(rB);
                     }
                 }
                 fence_before();
