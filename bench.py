@@ -41,10 +41,12 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="aniso_100k_d64")
+    p.add_argument("--workload", default="vmf_500k_d128")
     p.add_argument("--n", type=int, default=None, help="override the workload's row count")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "bf16_refined"])
+    p.add_argument("--precision", default="bf16_refined", choices=["fp32", "bf16_refined"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp32-compare", action="store_true",
+                   help="skip the plain f32 fit timed beside the bf16-refined one")
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the bounded oracle sample")
     return p.parse_args()
@@ -176,6 +178,15 @@ def cpu_baseline(x: np.ndarray, ms: int, cross_pairs: float, target_s: float) ->
     }
 
 
+# Ordered cross-component pairs summed over the Borůvka rounds of the exact fit of each named
+# workload at its full size (from the fit statistics; the exact fit is deterministic and the
+# same on every arithmetic path). The CPU reference arm extrapolates its per-pair cost with it.
+CROSS_PAIRS = {
+    "vmf_500k_d128": 942672776158.0,
+    "aniso_100k_d64": 31806079898.0,
+}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -185,11 +196,10 @@ def run_reference(args):
 
     x, ms, mcs = synthetic.workload(args.workload, n=args.n)
     n, d = x.shape
-    # cross-component pairs of the exact run are not known without a full fit; the Borůvka
-    # rounds of these workloads sum to about 3 n^2 ordered cross pairs on the device run
-    cross = 3.0 * n * n
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    cross = CROSS_PAIRS.get(args.workload) if args.n is None else None
+    cross_note = "recorded"
+    if cross is None:  # unrecorded size: the recorded workloads sum to about 3.8 n^2
+        cross, cross_note = 3.8 * n * n, "estimated as 3.8 n^2"
     times = []
     values = []
     for _ in range(args.steps):
@@ -203,7 +213,8 @@ def run_reference(args):
         "ms_per_step": float(np.median(times)) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "n": n, "d": d, "min_samples": ms,
-                   "min_cluster_size": mcs, "parallelism": "replicas"},
+                   "min_cluster_size": mcs, "parallelism": "replicas",
+                   "cross_pairs": cross, "cross_pairs_source": cross_note},
         "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": O.max_threads(),
                          "kind": "port", "sample": cb["sample"]},
         "e2e": {"value": value, "unit": "Mpts/s", "h2d_bytes_per_step": 0,
@@ -216,7 +227,7 @@ def run_ours(args):
     import torch
 
     import cuscan_gb300 as cg
-    from cuscan_gb300 import _lib, synthetic
+    from cuscan_gb300 import _lib, replicas, synthetic
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -232,7 +243,7 @@ def run_ours(args):
     x, ms, mcs = synthetic.workload(args.workload, n=args.n)
     if world > 1 and rank > 0:  # independent replica per rank
         gen, kw, _, _ = synthetic.WORKLOADS[args.workload]
-        kw = dict(kw, seed=kw["seed"] + 1000 * rank)
+        kw = dict(kw, seed=replicas.replica_seed(kw["seed"], rank))
         if args.n:
             kw["n"] = args.n
         x = gen(**kw)
@@ -279,13 +290,10 @@ def run_ours(args):
             assert m == n - 1
         barrier()
     launches = _lib.launch_count() - launches0
-    total_ms = float(np.sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
-    value = world * n * args.steps / (total_ms / 1e3) / 1e6
+    pts_per_s, worst_s = replicas.aggregate_throughput(n, args.steps, float(np.sum(step_ms)) / 1e3,
+                                                       device="cuda")
+    ms_per_step = worst_s * 1e3 / args.steps
+    value = pts_per_s / 1e6
 
     # end to end through the host-pointer C ABI (pinned host input and outputs)
     xh = torch.from_numpy(x).pin_memory().numpy()
@@ -296,13 +304,27 @@ def run_ours(args):
         t0 = time.perf_counter()
         ctx.fit_core(xh, ms, prec)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = float(np.sum(e2e_t))
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_pts_per_s, e2e_s = replicas.aggregate_throughput(n, args.steps, float(np.sum(e2e_t)),
+                                                         device="cuda")
     h2d = n * d * 4
     d2h = n * k * 8 + n * 4 + (n - 1) * 12
+
+    # the plain f32 form of the same fit, timed the same way (one step), for the comparison
+    fp32 = None
+    if args.precision == "bf16_refined" and not args.no_fp32_compare:
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.fit_core_device(xd.data_ptr(), n, d, ms, _lib.PRECISION_PLAIN, ids.data_ptr(),
+                            ksq.data_ptr(), core.data_ptr(), src.data_ptr(), dst.data_ptr(),
+                            wsq.data_ptr(), ctx.stream)
+        e1.record(stream)
+        e1.synchronize()
+        f_ms = e0.elapsed_time(e1)
+        fp32 = {"value": n / (f_ms / 1e3) / 1e6, "unit": "Mpts/s", "ms_per_step": f_ms,
+                "steps": 1, "bf16_refined_speedup": f_ms / ms_per_step}
 
     # roofline of the dominant kernel (CUDA events inside the fit, on its stream)
     bf16_peak, hbm_peak, peak_src = measured_peaks()
@@ -341,11 +363,13 @@ def run_ours(args):
                    "boruvka_fallback_rows": stats["boruvka_fallback_rows"],
                    "algorithmic_tflop_per_step": (w_knn + w_cand) / 1e12},
         "clocks": clocks.summary(),
-        "e2e": {"value": world * n * args.steps / e2e_s / 1e6, "unit": "Mpts/s",
+        "e2e": {"value": e2e_pts_per_s / 1e6, "unit": "Mpts/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roof,
     }
+    if fp32 is not None:
+        line["fp32_plain"] = fp32
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k2: v for k2, v in cpu_baseline(
             x, ms, stats["cross_pairs"], args.cpu_seconds).items() if k2 != "projected_fit_s"}
