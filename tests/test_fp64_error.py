@@ -1,0 +1,67 @@
+"""Error of the f32 fit core against an FP64 oracle (reported, loosely bounded).
+
+The reference decides neighbours, the MST and labels with f32 sequential-FMA distances; this
+build reproduces those bits exactly (the oracle tests). Against float64 arithmetic the f32 sum
+carries up to ~d * 2^-24 relative error on d^2; this test measures it for the core distances and
+for the total MST weight (the total weight of a minimum spanning tree is unique, so it is
+comparable across arithmetics even where tied edges differ).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from cuscan_gb300 import _lib, synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def f64_core_sq(x: np.ndarray, ms: int) -> np.ndarray:
+    x = x.astype(np.float64)
+    sq = (x * x).sum(1)
+    n = x.shape[0]
+    core = np.empty(n)
+    for a in range(0, n, 2048):
+        b = min(n, a + 2048)
+        d2 = sq[a:b, None] + sq[None, :] - 2.0 * x[a:b] @ x.T
+        np.maximum(d2, 0.0, out=d2)
+        d2[np.arange(b - a), np.arange(a, b)] = np.inf  # exclude self
+        core[a:b] = np.partition(d2, ms - 1, axis=1)[:, ms - 1]
+    return core
+
+
+def f64_mst_weight(x: np.ndarray, core_sq: np.ndarray) -> float:
+    """Prim's algorithm on the f64 mutual-reachability graph; returns sum of sqrt(w)."""
+    x = x.astype(np.float64)
+    n = x.shape[0]
+    in_tree = np.zeros(n, bool)
+    best = np.full(n, np.inf)
+    cur = 0
+    total = 0.0
+    for _ in range(n - 1):
+        in_tree[cur] = True
+        diff = x - x[cur]
+        d2 = np.einsum("ij,ij->i", diff, diff)
+        w = np.maximum(np.maximum(d2, core_sq[cur]), core_sq)
+        np.minimum(best, w, out=best)
+        best[in_tree] = np.inf
+        cur = int(np.argmin(best))
+        total += np.sqrt(best[cur])
+    return total
+
+
+@pytest.mark.parametrize("name,n", [("vmf_500k_d128", 8000), ("aniso_100k_d64", 8000)])
+def test_core_and_mst_weight_error_vs_fp64(gpu_ctx, name, n, capsys):
+    x, ms, _ = synthetic.workload(name, n=n)
+    out = gpu_ctx.fit_core(x, ms, _lib.PRECISION_BF16_REFINED)
+    core64 = f64_core_sq(x, ms)
+    core32 = out["core_sq"].astype(np.float64)
+    rel_core = np.max(np.abs(np.sqrt(core32) - np.sqrt(core64)) / np.sqrt(core64))
+    w32 = float(np.sqrt(out["wsq"].astype(np.float64)).sum())
+    w64 = f64_mst_weight(x, core64)
+    rel_w = abs(w32 - w64) / w64
+    with capsys.disabled():
+        print(f"\n[fp64] {name} n={n}: max rel error core distance {rel_core:.3e}, "
+              f"total MST weight {rel_w:.3e}")
+    assert rel_core < 1e-5
+    assert rel_w < 1e-5
