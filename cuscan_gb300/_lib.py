@@ -39,6 +39,9 @@ SIGNATURES = {
                                             _VP]),
     "cuscan_component_reduce": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int64,
                                           C.c_int64, C.c_int64, _VP, _VP, _VP]),
+    "cuscan_component_reduce_noalloc": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int64,
+                                                  C.c_int64, C.c_int64, _VP, _VP, _VP,
+                                                  C.c_char_p, C.c_size_t]),
     "cuscan_fit_core": (C.c_int, [_VP, _F32P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, _I32P,
                                   _F32P, _F32P, _U32P, _U32P, _F32P, _I64P, _VP]),
     "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
@@ -117,6 +120,21 @@ def load(build_if_missing: bool = True):
 def launch_count() -> int:
     """Kernels launched by the library in this process so far."""
     return int(load().cuscan_launch_count())
+
+
+NOALLOC_MAX_TILES = 65536
+
+
+def component_reduce_noalloc(weights, indices, members, tile_starts, tile_ends, partial_offsets,
+                             n, p, c, win_weights, win_meta, stream=None):
+    """cuscan_component_reduce_noalloc on device pointers: the variant that allocates nothing
+    (its tile scratch is a fixed static device array of NOALLOC_MAX_TILES entries)."""
+    lib = load()
+    err = C.create_string_buffer(256)
+    code = lib.cuscan_component_reduce_noalloc(weights, indices, members, tile_starts, tile_ends,
+                                               partial_offsets, n, p, c, win_weights, win_meta,
+                                               stream, err, 256)
+    raise_for(code, err.value.decode("utf-8", "replace"))
 
 
 def raise_for(code: int, message: str):

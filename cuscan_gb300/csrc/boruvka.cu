@@ -11,6 +11,8 @@
 // The fused fit path calls the kernel on component-sorted rows. A (query block, reference
 // tile) pair whose rows all carry one label holds only same-component pairs and is skipped
 // before any distance is computed; tile label ranges are precomputed per 32-row tile.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace cuscan {
@@ -368,4 +370,96 @@ int launch_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t
     return CUSCAN_OK;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Component reduction without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they need this reduction: a host
+// whose device memory is owned by another framework's caching pool, a real-time loop that must
+// not take the implicit synchronisation of cudaMalloc/cudaFree, or a plugin that is handed
+// device buffers and nothing else. For them the per-tile partial results live in a fixed
+// array of static device memory that the CUDA module owns: every GPU that loads this library
+// keeps NOALLOC_MAX_TILES * 16 bytes (1 MiB) for it until the process exits.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t NOALLOC_MAX_TILES = 65536;  // == CUSCAN_NOALLOC_MAX_TILES in the header
+
+static __device__ __align__(256) Fold g_noalloc_partials[NOALLOC_MAX_TILES];
+
+// The array's address on each device. In host code the symbol is only a host-side stand-in;
+// the device address is fetched once per device with that device current.
+std::mutex g_noalloc_mutex;
+Fold *g_noalloc_ptr[64] = {};
+
+void set_err(char *err, size_t len, const char *msg) {
+    if (err && len) {
+        snprintf(err, len, "%s", msg);
+    }
+}
+
+}  // namespace
+
 }  // namespace cuscan
+
+extern "C" int cuscan_component_reduce_noalloc(
+    const float *weights, const int32_t *indices, const int32_t *members,
+    const int32_t *tile_starts, const int32_t *tile_ends, const int32_t *partial_offsets,
+    int64_t n, int64_t p, int64_t c, float *win_weights, int32_t *win_meta, void *stream,
+    char *err, size_t err_len) {
+    using namespace cuscan;
+    if (n < 0 || p < 0 || c < 0 || c > n || p > n) {
+        set_err(err, err_len, "component_reduce_noalloc received inconsistent sizes");
+        return CUSCAN_INVALID_INPUT;
+    }
+    if (n > INT32_MAX) {
+        set_err(err, err_len, "component member index exceeds the supported integer range");
+        return CUSCAN_OVERFLOW;
+    }
+    if (p > NOALLOC_MAX_TILES) {
+        char msg[160];
+        snprintf(msg, sizeof(msg),
+                 "component_reduce_noalloc supports at most %lld tiles (got %lld); use "
+                 "cuscan_component_reduce for larger plans",
+                 (long long)NOALLOC_MAX_TILES, (long long)p);
+        set_err(err, err_len, msg);
+        return CUSCAN_CAPACITY;
+    }
+    if (c == 0) return CUSCAN_OK;
+    int device = -1;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess || device < 0 || device >= 64) {
+        cudaGetLastError();
+        set_err(err, err_len, "no usable current CUDA device");
+        return CUSCAN_BACKEND_UNAVAILABLE;
+    }
+    Fold *scratch = nullptr;
+    {
+        // first call on a device: resolve the static array's device address (done once)
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[device]) {
+            void *ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_noalloc_partials);
+            if (e != cudaSuccess || !ptr) {
+                cudaGetLastError();
+                set_err(err, err_len, "cudaGetSymbolAddress of the static partials failed");
+                return CUSCAN_BACKEND_UNAVAILABLE;
+            }
+            g_noalloc_ptr[device] = static_cast<Fold *>(ptr);
+        }
+        scratch = g_noalloc_ptr[device];
+    }
+    // every tile writes its own partial, so no clearing of the shared array is needed
+    cudaStream_t s = (cudaStream_t)stream;
+    if (p > 0) {
+        CUSCAN_KERNEL(reduce_tiles_kernel, (unsigned)ceil_div(p * 32, 256), 256, 0, s, weights,
+                      indices, members, tile_starts, tile_ends, p, (uint32_t)n, scratch);
+    }
+    CUSCAN_KERNEL(reduce_components_kernel, (unsigned)ceil_div(c * 32, 256), 256, 0, s, weights,
+                  indices, partial_offsets, scratch, c, (uint32_t)n, win_weights, win_meta);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_err(err, err_len, cudaGetErrorString(e));
+        return CUSCAN_BACKEND_UNAVAILABLE;
+    }
+    return CUSCAN_OK;
+}

@@ -129,6 +129,28 @@ int cuscan_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t
                             void *stream);
 
 /*
+ * cuscan_component_reduce without any device allocation (no counterpart in the reference; an
+ * addition for callers that cannot allocate device memory, e.g. because another framework's
+ * caching pool owns it, or because the implicit synchronisation of cudaMalloc/cudaFree is not
+ * acceptable on their path). Same inputs, outputs and results as cuscan_component_reduce; no
+ * context is needed. The per-tile scratch is a static device array of
+ * CUSCAN_NOALLOC_MAX_TILES entries (1 MiB) that every GPU loading this library holds until
+ * exit; plans with more tiles (p) are rejected with CUSCAN_CAPACITY.
+ *  - The first call on a device, with that device current, resolves the array's address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - Every call shares the one array: calls that overlap on the GPU (different streams, or
+ *    different host threads on the same device) race and must be serialised by the caller.
+ *  - stream is a cudaStream_t as void* (NULL = the legacy default stream); err (may be NULL)
+ *    receives the message of a failure.
+ */
+#define CUSCAN_NOALLOC_MAX_TILES 65536
+int cuscan_component_reduce_noalloc(const float *weights, const int32_t *indices,
+                                    const int32_t *members, const int32_t *tile_starts,
+                                    const int32_t *tile_ends, const int32_t *partial_offsets,
+                                    int64_t n, int64_t p, int64_t c, float *win_weights,
+                                    int32_t *win_meta, void *stream, char *err, size_t err_len);
+
+/*
  * Fused exact fit core of the brute-force complete-graph route: kNN core distances
  * (k = min(min_samples, n-1)), kNN seed forest, then Borůvka rounds until one component
  * remains, all on the device. Inputs and outputs are HOST pointers; the function copies the
