@@ -247,12 +247,19 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
     }
 }
 
-// Order in which query block qb visits the reference tiles: starting with the tile that holds
-// the block itself and wrapping around. In cell-sorted data the first tiles hold the block's
-// nearest neighbours, so the per-row thresholds tighten early and later tiles rarely hit.
+// Order in which query block qb visits the reference tiles: first a window of WARM tiles around
+// the block's own tile (in cell-sorted data these hold the block's nearest neighbours, so the
+// per-row thresholds tighten at once), then every other tile in one global order shared by all
+// CTAs, so that the blocks running at the same time stream the same tiles and share them in L2.
+constexpr int64_t WARM = 4;
 __device__ __forceinline__ int64_t tile_order(const Params &P, int64_t qb, int64_t i) {
-    int64_t t = (qb * BM) / BN + i;
-    return t >= P.n_tiles ? t - P.n_tiles : t;
+    const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
+    int64_t a = (qb * BM) / BN - w / 2;
+    if (a < 0) a = 0;
+    if (a > P.n_tiles - w) a = P.n_tiles - w;
+    if (i < w) return a + i;
+    const int64_t j = i - w;
+    return j < a ? j : j + w;
 }
 
 // Label range of query block qb (4 chunks of 32 rows).
