@@ -43,12 +43,22 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="vmf_500k_d128")
     p.add_argument("--n", type=int, default=None, help="override the workload's row count")
-    p.add_argument("--precision", default="bf16_refined", choices=["fp32", "bf16_refined"])
+    p.add_argument("--precision", default="bf16_refined",
+                   choices=["fp32", "bf16_refined", "fp16_refined"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp32-compare", action="store_true",
                    help="skip the plain f32 fit timed beside the bf16-refined one")
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the bounded oracle sample")
+    p.add_argument("--no-serve", action="store_true", help="skip the fit-request serving run")
+    p.add_argument("--serve-only", action="store_true", help="run only the serving benchmark")
+    p.add_argument("--serve-requests", type=int, default=10000)
+    p.add_argument("--serve-pool", type=int, default=256,
+                   help="distinct point sets the request stream cycles through")
+    p.add_argument("--serve-slots", type=int, default=8)
+    p.add_argument("--serve-precisions", default="bf16_refined,fp16_refined,fp32")
+    p.add_argument("--serve-load", type=float, default=0.7,
+                   help="Poisson arrival rate as a fraction of the measured saturation rate")
     return p.parse_args()
 
 
@@ -188,6 +198,138 @@ CROSS_PAIRS = {
 }
 
 
+def serving_run(args, precision: str) -> dict:
+    """Fit-request serving: a stream of Gaussian-mixture fits (n log-uniform in [500, 50000],
+    d in {16, 32, 64, 128}) through the continuous-batching server. First the saturation rate
+    (every request queued at once), then Poisson arrivals at `serve_load` times that rate with
+    latency = arrival -> labels ready on the host."""
+    import torch
+
+    from cuscan_gb300 import synthetic
+    from cuscan_gb300.serving import FitServer
+
+    specs = synthetic.fit_request_stream(args.serve_requests)
+    pool_n = min(args.serve_pool, len(specs))
+    pool = [synthetic.request_points(specs[i]) for i in range(pool_n)]
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(0.5 * free)
+
+    def kwargs(i):
+        sp = specs[i % pool_n]
+        return dict(min_cluster_size=sp["min_cluster_size"], min_samples=sp["min_samples"],
+                    precision=precision)
+
+    def run(count, rate, srv):
+        """Submit `count` requests (all at once if rate is None, else Poisson arrivals) and
+        collect every completion; returns per-request latency (ms) and the makespan (s)."""
+        rng = np.random.default_rng(7)
+        arrivals = (np.zeros(count) if rate is None
+                    else np.cumsum(rng.exponential(1.0 / rate, size=count)))
+        lag = {}
+        lat, queued, points, failures, recs = [], [], 0, 0, []
+        done = threading.Event()
+        errors = []
+
+        def collect():
+            nonlocal points, failures
+            got = 0
+            try:
+                while got < count:
+                    rid = srv.wait_any(5.0)
+                    if rid is None:
+                        continue
+                    info = srv.wait(rid, 0.0)
+                    for _ in range(100000):
+                        if rid in lag:
+                            break
+                        time.sleep(1e-4)
+                    lat.append(lag[rid] + info["latency_ms"])
+                    queued.append(info["queued_ms"])
+                    st = info["stats"]
+                    recs.append((info["n"], lat[-1], info["run_ms"], info["prep_ms"],
+                                 info["fit_ms"], info["extract_ms"],
+                                 st["core_ms"] + st["mst_ms"]))
+                    points += info["n"]
+                    failures += info["status"] != 0
+                    srv.release(rid)
+                    got += 1
+            except BaseException as exc:  # surfaced by the submitting thread
+                errors.append(exc)
+            finally:
+                done.set()
+
+        th = threading.Thread(target=collect, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        for i in range(count):
+            if errors:
+                break
+            target = t0 + arrivals[i]
+            now = time.perf_counter()
+            if target > now:
+                time.sleep(target - now)
+            sub = time.perf_counter()
+            rid = srv.submit(pool[i % pool_n], **kwargs(i))
+            lag[rid] = max(0.0, (sub - target) * 1e3)
+        if not done.wait(timeout=600.0):
+            raise RuntimeError("serving run did not finish within 600 s")
+        makespan = time.perf_counter() - t0
+        th.join()
+        if errors:
+            raise errors[0]
+        return np.asarray(lat), np.asarray(queued), points, failures, makespan, np.asarray(recs)
+
+    def by_size(recs):
+        """Latency and where a request's time goes, per size class of n."""
+        out = {}
+        for lo, hi in ((500, 2000), (2000, 10000), (10000, 50001)):
+            r = recs[(recs[:, 0] >= lo) & (recs[:, 0] < hi)]
+            if len(r) == 0:
+                continue
+            out[f"n{lo}-{hi - 1}"] = {
+                "requests": int(len(r)), "p50_ms": float(np.percentile(r[:, 1], 50)),
+                "p99_ms": float(np.percentile(r[:, 1], 99)),
+                "mean_run_ms": float(r[:, 2].mean()), "mean_prep_ms": float(r[:, 3].mean()),
+                "mean_fit_ms": float(r[:, 4].mean()), "mean_extract_ms": float(r[:, 5].mean()),
+                "mean_gpu_event_ms": float(r[:, 6].mean())}
+        return out
+
+    with FitServer(slots=args.serve_slots, budget_bytes=budget) as srv:
+        warm = [srv.submit(pool[i % pool_n], **kwargs(i)) for i in range(2 * args.serve_slots)]
+        for r in warm:
+            srv.result(r, timeout=300.0)
+        sat_count = min(len(specs), 2000)
+        lat_s, _, pts_s, fail_s, span_s, _ = run(sat_count, None, srv)
+        capacity = sat_count / span_s
+        rate = args.serve_load * capacity
+        lat, queued, pts, fails, span, recs = run(len(specs), rate, srv)
+        st = srv.stats()
+    return {
+        "precision": precision, "requests": len(specs), "distinct_point_sets": pool_n,
+        "slots": args.serve_slots, "budget_bytes": budget,
+        "saturation": {"requests": sat_count, "req_per_s": capacity,
+                       "mpts_per_s": pts_s / span_s / 1e6, "failures": int(fail_s)},
+        "poisson": {"rate_req_per_s": rate, "load": args.serve_load,
+                    "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
+                    "mean_ms": float(lat.mean()),
+                    "queue_p99_ms": float(np.percentile(queued, 99)),
+                    "req_per_s": len(specs) / span, "mpts_per_s": pts / span / 1e6,
+                    "failures": int(fails), "by_size": by_size(recs)},
+        "peak_committed_bytes": st["peak_committed_bytes"],
+        "workspace_releases": st["workspace_releases"],
+    }
+
+
+def serving_section(args) -> dict:
+    out = {"workload": "gaussian mixtures, n log-uniform [500, 50000], d in {16,32,64,128}, "
+                       "2-30 blobs (std U[0.5,2]), min_samples 5, min_cluster_size max(5, n/200)",
+           "latency": "arrival -> labels and strengths ready on the host"}
+    for prec in args.serve_precisions.split(","):
+        out[prec] = serving_run(args, prec)
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -241,6 +383,10 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
+    if args.serve_only:
+        if rank == 0:
+            print(json.dumps({"serving": serving_section(args)}), flush=True)
+        return
     x, ms, mcs = synthetic.workload(args.workload, n=args.n)
     if world > 1 and rank > 0:  # independent replica per rank
         gen, kw, _, _ = synthetic.WORKLOADS[args.workload]
@@ -250,7 +396,7 @@ def run_ours(args):
         x = gen(**kw)
     n, d = x.shape
     k = min(ms, n - 1)
-    prec = _lib.PRECISION_BF16_REFINED if args.precision == "bf16_refined" else _lib.PRECISION_PLAIN
+    prec = _lib.PRECISIONS[args.precision]
     ctx = cg.context(local)
 
     xd = torch.from_numpy(x).cuda()
@@ -312,7 +458,7 @@ def run_ours(args):
 
     # the plain f32 form of the same fit, timed the same way (one step), for the comparison
     fp32 = None
-    if args.precision == "bf16_refined" and not args.no_fp32_compare:
+    if args.precision != "fp32" and not args.no_fp32_compare:
         flush.zero_()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -325,7 +471,7 @@ def run_ours(args):
         e1.synchronize()
         f_ms = e0.elapsed_time(e1)
         fp32 = {"value": n / (f_ms / 1e3) / 1e6, "unit": "Mpts/s", "ms_per_step": f_ms,
-                "steps": 1, "bf16_refined_speedup": f_ms / ms_per_step}
+                "steps": 1, f"{args.precision}_speedup": f_ms / ms_per_step}
 
     # roofline of the dominant kernel (CUDA events inside the fit, on its stream)
     bf16_peak, hbm_peak, peak_src = measured_peaks()
@@ -351,7 +497,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
+        "dtype": {"fp32": "f32", "bf16_refined": "bf16+f32", "fp16_refined": "fp16+f32"}[args.precision],
         "data": "synthetic",
         "config": {"workload": args.workload, "n": n, "d": d, "min_samples": ms,
                    "min_cluster_size": mcs, "precision": args.precision,
@@ -373,6 +519,10 @@ def run_ours(args):
     }
     if fp32 is not None:
         line["fp32_plain"] = fp32
+    if rank == 0 and world == 1 and not args.no_serve:
+        del xd, ids, ksq, core, src, dst, wsq, flush
+        torch.cuda.empty_cache()
+        line["serving"] = serving_section(args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k2: v for k2, v in cpu_baseline(
             x, ms, stats["cross_pairs"], args.cpu_seconds).items() if k2 != "projected_fit_s"}

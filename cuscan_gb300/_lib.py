@@ -14,8 +14,11 @@ from pathlib import Path
 import numpy as np
 
 OK, INVALID_CONFIG, INVALID_INPUT, BACKEND_UNAVAILABLE, NUMERICAL, OVERFLOW, CAPACITY, MEMORY = range(8)
+PENDING = 8  # not an error: a server request is still queued or running
 PRECISION_PLAIN = 0
 PRECISION_BF16_REFINED = 1
+PRECISION_FP16_REFINED = 2
+PRECISIONS = {"fp32": 0, "bf16_refined": 1, "fp16_refined": 2}
 
 _F32P = C.POINTER(C.c_float)
 _F64P = C.POINTER(C.c_double)
@@ -55,6 +58,22 @@ SIGNATURES = {
                                       _F32P]),
     "cuscan_clustering_free": (None, [_VP]),
     "cuscan_dbscan_cut": (C.c_int, [_F64P, C.c_int64, C.c_double, C.c_int64, _I32P]),
+    "cuscan_fit_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int32, C.c_int32, C.c_int32]),
+    "cuscan_ctx_reserved_bytes": (C.c_int64, [_VP]),
+    "cuscan_ctx_release_workspace": (C.c_int, [_VP]),
+    "cuscan_server_create": (C.c_int, [C.c_int, C.c_int32, C.c_int64, C.POINTER(_VP),
+                                       C.c_char_p, C.c_size_t]),
+    "cuscan_server_create_simulated": (C.c_int, [C.c_int32, C.c_int64, C.c_double,
+                                                 C.POINTER(_VP), C.c_char_p, C.c_size_t]),
+    "cuscan_server_destroy": (None, [_VP]),
+    "cuscan_server_submit_fit": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                           _VP, _I64P]),
+    "cuscan_server_wait": (C.c_int, [_VP, C.c_int64, C.c_double, _VP]),
+    "cuscan_server_wait_any": (C.c_int, [_VP, C.c_double, _I64P]),
+    "cuscan_server_read_fit": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
+    "cuscan_server_request_error": (C.c_int, [_VP, C.c_int64, C.c_char_p, C.c_size_t]),
+    "cuscan_server_release": (C.c_int, [_VP, C.c_int64]),
+    "cuscan_server_get_stats": (C.c_int, [_VP, _VP]),
 }
 
 
@@ -86,6 +105,52 @@ class ExtractConfig(C.Structure):
         ("cluster_selection_epsilon", C.c_double),
         ("cluster_selection_persistence", C.c_double),
     ]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [
+        ("request_id", C.c_int64),
+        ("status", C.c_int32),
+        ("slot", C.c_int32),
+        ("n", C.c_int64),
+        ("finite_rows", C.c_int64),
+        ("d", C.c_int32),
+        ("n_clusters", C.c_int32),
+        ("workspace_bound_bytes", C.c_int64),
+        ("submit_ms", C.c_double),
+        ("queued_ms", C.c_double),
+        ("run_ms", C.c_double),
+        ("latency_ms", C.c_double),
+        ("done_ms", C.c_double),
+        ("prep_ms", C.c_double),
+        ("fit_ms", C.c_double),
+        ("extract_ms", C.c_double),
+        ("stats", FitStats),
+    ]
+
+    def as_dict(self) -> dict:
+        out = {name: getattr(self, name) for name, _ in self._fields_ if name != "stats"}
+        out["stats"] = self.stats.as_dict()
+        return out
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("slots", C.c_int32),
+        ("pad", C.c_int32),
+        ("budget_bytes", C.c_int64),
+        ("submitted", C.c_int64),
+        ("completed", C.c_int64),
+        ("failed", C.c_int64),
+        ("queued", C.c_int64),
+        ("running", C.c_int64),
+        ("committed_bytes", C.c_int64),
+        ("peak_committed_bytes", C.c_int64),
+        ("workspace_releases", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "pad"}
 
 
 _lock = threading.Lock()
@@ -137,6 +202,11 @@ def component_reduce_noalloc(weights, indices, members, tile_starts, tile_ends, 
     raise_for(code, err.value.decode("utf-8", "replace"))
 
 
+def fit_workspace_bytes(n: int, d: int, min_samples: int, precision: int) -> int:
+    """Upper bound on the device workspace of one fit (cuscan_fit_workspace_bytes)."""
+    return int(load().cuscan_fit_workspace_bytes(int(n), int(d), int(min_samples), int(precision)))
+
+
 def raise_for(code: int, message: str):
     if code == OK:
         return
@@ -168,6 +238,13 @@ class Context:
         if getattr(self, "handle", None):
             self._lib.cuscan_ctx_destroy(self.handle)
             self.handle = None
+
+    def reserved_bytes(self) -> int:
+        """Device bytes this context's workspace holds."""
+        return int(self._lib.cuscan_ctx_reserved_bytes(self.handle))
+
+    def release_workspace(self):
+        self.check(self._lib.cuscan_ctx_release_workspace(self.handle))
 
     def __del__(self):
         try:

@@ -27,6 +27,18 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                               int64_t *fallback_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
                       float *out, cudaStream_t s);
+size_t refined_workspace_bytes(int64_t n, int d, int k);
+
+// Every device buffer a context holds.
+static int workspace_buffers(FitWorkspace *f, Buffer **out) {
+    Buffer *own[] = {&f->x, &f->ids, &f->dsq, &f->core, &f->label, &f->src, &f->dst, &f->w,
+                     &f->op_keys, &f->op_tiles_lo, &f->op_tiles_hi, &f->op_partials,
+                     &f->op_knn_ids, &f->op_knn_dist};
+    const int n_own = (int)(sizeof(own) / sizeof(own[0]));
+    for (int i = 0; i < n_own; ++i) out[i] = own[i];
+    return n_own + forest_buffers(f->forest, out + n_own);
+}
+constexpr int kWorkspaceBufferCount = 14 + kForestBufferCount;
 
 }  // namespace cuscan
 
@@ -82,11 +94,10 @@ void cuscan_ctx_destroy(cuscan_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->fit) {
         FitWorkspace *f = ctx->fit;
-        forest_release(f->forest);
-        Buffer *all[] = {&f->x, &f->ids, &f->dsq, &f->core, &f->label, &f->src, &f->dst, &f->w,
-                         &f->op_keys, &f->op_tiles_lo, &f->op_tiles_hi, &f->op_partials,
-                         &f->op_knn_ids, &f->op_knn_dist};
-        for (Buffer *b : all) release(*b);
+        Buffer *all[kWorkspaceBufferCount];
+        const int count = workspace_buffers(f, all);
+        for (int i = 0; i < count; ++i) release(*all[i]);
+        f->forest.status = nullptr;
         if (f->host_status) cudaFreeHost(f->host_status);
         for (auto &ev : f->ev)
             if (ev) cudaEventDestroy(ev);
@@ -94,6 +105,41 @@ void cuscan_ctx_destroy(cuscan_ctx *ctx) {
     }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+}
+
+int64_t cuscan_ctx_reserved_bytes(const cuscan_ctx *ctx) {
+    if (!ctx || !ctx->fit) return 0;
+    Buffer *all[kWorkspaceBufferCount];
+    const int count = workspace_buffers(ctx->fit, all);
+    int64_t total = 0;
+    for (int i = 0; i < count; ++i) total += (int64_t)all[i]->bytes;
+    return total;
+}
+
+int cuscan_ctx_release_workspace(cuscan_ctx *ctx) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    Buffer *all[kWorkspaceBufferCount];
+    const int count = workspace_buffers(ctx->fit, all);
+    for (int i = 0; i < count; ++i) release(*all[i]);
+    ctx->fit->forest.status = nullptr;
+    return CUSCAN_OK;
+}
+
+int64_t cuscan_fit_workspace_bytes(int64_t n, int32_t d, int32_t min_samples, int32_t precision) {
+    if (n < 2 || d <= 0 || min_samples <= 0) return 0;
+    const size_t N = (size_t)n, D = (size_t)d;
+    const size_t k = (size_t)((int64_t)min_samples < n - 1 ? min_samples : n - 1);
+    size_t b = 4 * N * D + 8 * N * k + 5 * 4 * N;  // input copy, kNN lists, core/label/MST arrays
+    b += 18 * 4 * N + 4 * N * D + 16 * N;          // forest arrays, sorted copy, 64-bit keys
+    b += 2 * 4 * (N / 32 + 2) + 64 + sizeof(DevStatus) + 4 * (N / 1024 + 2);  // tiles, scan
+    // split-kNN partial lists: at most 2 * SMs + query blocks blocks of 128 rows
+    b += 8 * k * 128 * (size_t)(2 * 2 * kSMs + ceil_div(n, 128));
+    if (precision == CUSCAN_PRECISION_BF16_REFINED || precision == CUSCAN_PRECISION_FP16_REFINED)
+        b += refined_workspace_bytes(n, d, (int)k);
+    return (int64_t)b + (1 << 20);
 }
 
 const char *cuscan_last_error(const cuscan_ctx *ctx) { return ctx ? ctx->err : "null context"; }
@@ -196,11 +242,13 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     if (n > INT32_MAX - 1)
         return fail(ctx, CUSCAN_INVALID_INPUT, "row count %lld exceeds the supported maximum",
                     (long long)n);
-    if (precision != CUSCAN_PRECISION_PLAIN && precision != CUSCAN_PRECISION_BF16_REFINED)
+    if (precision != CUSCAN_PRECISION_PLAIN && precision != CUSCAN_PRECISION_BF16_REFINED &&
+        precision != CUSCAN_PRECISION_FP16_REFINED)
         return fail(ctx, CUSCAN_INVALID_CONFIG, "unknown precision %d", precision);
-    if (precision == CUSCAN_PRECISION_BF16_REFINED && !refined_available())
+    const bool refined = precision != CUSCAN_PRECISION_PLAIN;
+    if (refined && !refined_available())
         return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE,
-                    "bf16-refined sweeps are not available for this shape");
+                    "refined sweeps are not available for this shape");
     if (!data || !knn_ids || !knn_sq || !core_sq || !mst_src || !mst_dst || !mst_wsq)
         return fail(ctx, CUSCAN_INVALID_INPUT, "fit_core_device received a null pointer");
     CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -214,11 +262,13 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     int32_t *label = as<int32_t>(f->label);
     cudaEvent_t *ev = f->ev;
     int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0;
+    b.refined.want_fp16 = precision == CUSCAN_PRECISION_FP16_REFINED;
+    b.refined.have_scale = false;
 
     CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
     // ---- core_distances: exact kNN sweep (estimator.rs:591-657) + core column ----
-    if (precision == CUSCAN_PRECISION_BF16_REFINED)
+    if (refined)
         rc = launch_knn_refined(ctx, b, data, n, d, k, knn_ids, knn_sq, s, &refined_rows,
                                 &fallback_rows);
     else
@@ -246,7 +296,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         unsigned long long *row_keys = as<unsigned long long>(b.row_keys);
         if ((rc = launch_fill_u64(ctx, row_keys, n, ~0ull, s))) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[4], s));
-        if (precision == CUSCAN_PRECISION_BF16_REFINED)
+        if (refined)
             rc = launch_candidates_refined(ctx, b, n, d, knn_ids, knn_sq, k, core_sq, label, s,
                                            &boruvka_fallback_rows);
         else
@@ -256,7 +306,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if (rc) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[5], s));
         if ((rc = forest_round(ctx, b, n, components, label, mst_src, mst_dst, mst_wsq, s,
-                               precision == CUSCAN_PRECISION_BF16_REFINED)))
+                               refined)))
             return rc;
         if ((rc = read_status(ctx, b.status, hs, s))) return rc;
         cand_ms += elapsed(ev[4], ev[5]);

@@ -328,8 +328,7 @@ int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core
         return fail(ctx, CUSCAN_CAPACITY,
                     "feature count %d exceeds the shared-memory staging limit of the Boruvka "
                     "kernel (at most 256 features)", d);
-    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(candidates_fp32_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = allow_dynamic_smem(ctx, candidates_fp32_kernel, smem)) return rc;
     dim3 grid((unsigned)qblocks, (unsigned)splits);
     CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d,
                   tile_lo, tile_hi, chunk, row_keys, qmap, nq);

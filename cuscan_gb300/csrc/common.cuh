@@ -76,6 +76,25 @@ inline int cuda_fail(cuscan_ctx *ctx, cudaError_t e, const char *what) {
         if (_e != cudaSuccess) return ::cuscan::cuda_fail((ctx), _e, what); \
     } while (0)
 
+// Raise a kernel's dynamic shared-memory cap to the device's opt-in limit. Every call sets the
+// same value, so a fit running on another host thread cannot lower the cap between this call
+// and a launch that needs more (the attribute belongs to the kernel, not to a stream).
+template <class Kernel>
+inline int allow_dynamic_smem(cuscan_ctx *ctx, Kernel kernel, size_t bytes) {
+    int optin = 0;
+    CUSCAN_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                            ctx->device));
+    cudaFuncAttributes attr;
+    CUSCAN_CUDA(ctx, cudaFuncGetAttributes(&attr, (const void *)kernel));
+    const size_t cap = (size_t)optin - attr.sharedSizeBytes;
+    if (bytes > cap)
+        return fail(ctx, CUSCAN_CAPACITY, "a kernel needs %zu bytes of shared memory, the device "
+                    "allows %zu", bytes, cap);
+    CUSCAN_CUDA(ctx, cudaFuncSetAttribute((const void *)kernel,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap));
+    return CUSCAN_OK;
+}
+
 // Number of kernels this library has launched in the process (reported by
 // cuscan_launch_count so callers can account for every launch of a timed region).
 inline std::atomic<long long> &launch_counter() {

@@ -516,18 +516,26 @@ int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d) {
     return CUSCAN_OK;
 }
 
-void forest_release(ForestBuffers &b) {
+int forest_buffers(ForestBuffers &b, Buffer **out) {
+    RefinedBuffers &r = b.refined;
     Buffer *all[] = {&b.next, &b.esrc, &b.edst, &b.ew, &b.jmp_a, &b.mx_a, &b.jmp_b, &b.mx_b,
                      &b.keep, &b.pos, &b.parent, &b.minlab, &b.kept_total, &b.cnt, &b.start,
                      &b.fill, &b.perm, &b.xp, &b.corep, &b.labp, &b.row_keys, &b.comp_keys,
                      &b.tile_lo, &b.tile_hi, &b.status_buf, &b.scan_tmp, &b.knn_ids_tmp,
-                     &b.knn_dist_tmp};
-    for (Buffer *p : all) release(*p);
-    RefinedBuffers &r = b.refined;
-    Buffer *rall[] = {&r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo, &r.tile_hi,
-                      &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
-                      &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d};
-    for (Buffer *p : rall) release(*p);
+                     &b.knn_dist_tmp, &r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo,
+                     &r.tile_hi, &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
+                     &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d, &r.absmax};
+    static_assert(sizeof(all) / sizeof(all[0]) == kForestBufferCount, "buffer list");
+    const int count = (int)(sizeof(all) / sizeof(all[0]));
+    if (out)
+        for (int i = 0; i < count; ++i) out[i] = all[i];
+    return count;
+}
+
+void forest_release(ForestBuffers &b) {
+    Buffer *all[kForestBufferCount];
+    const int count = forest_buffers(b, all);
+    for (int i = 0; i < count; ++i) release(*all[i]);
     b.status = nullptr;
 }
 

@@ -17,7 +17,12 @@ struct DevStatus {
 // Buffers of the bf16 screening path (refined.cu).
 struct RefinedBuffers {
     Buffer xt, pnorm, mnorm, tile_mmax, tile_lo, tile_hi, cand_ids, cand_lb, fallback, count;
-    Buffer error, cbound, rowcnt, pivots, cells, cell_d;
+    Buffer error, cbound, rowcnt, pivots, cells, cell_d, absmax;
+    // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
+    bool want_fp16 = false;  // requested by the caller's precision
+    bool fp16 = false;       // in use (the data's range allows a scale)
+    bool have_scale = false; // scale computed for the current fit
+    float scale = 1.0f;
 };
 
 struct ForestBuffers {
@@ -36,6 +41,9 @@ struct ForestBuffers {
 
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
 void forest_release(ForestBuffers &b);
+// Every device buffer of the forest and of the bf16 screen (out may be null); returns the count.
+constexpr int kForestBufferCount = 45;
+int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);
 // Seed forest (mst.rs:368-420): appends the kept seed edges and labels points by the smallest

@@ -294,8 +294,7 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
     int64_t chunk = ceil_div(ceil_div(nr, splits), RT) * RT;
     splits = ceil_div(nr, chunk);
     const size_t smem = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
-    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(knn_fp32_kernel<K>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = allow_dynamic_smem(ctx, knn_fp32_kernel<K>, smem)) return rc;
     dim3 grid((unsigned)qblocks, (unsigned)splits);
     if (splits == 1) {
         CUSCAN_KERNEL(knn_fp32_kernel<K>, grid, QB, smem, s, query, nq, ref, nr, d, k,
@@ -348,8 +347,7 @@ int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const
     if (qmap) return fail(ctx, CUSCAN_CAPACITY, "row-subset kNN supports k <= 32");
     const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
     const size_t smem = ((size_t)d * QB + (size_t)d * RTP) * sizeof(float);
-    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(knn_fp32_wide_kernel,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = allow_dynamic_smem(ctx, knn_fp32_wide_kernel, smem)) return rc;
     CUSCAN_KERNEL(knn_fp32_wide_kernel, (unsigned)ceil_div(nq, QB), QB, smem, s,
         query, nq, ref, nr, d, k, exclude_self, query_offset, pad, ids, dist);
     CUSCAN_LAUNCH(ctx, "knn_fp32_wide_kernel");

@@ -41,7 +41,7 @@ constexpr int VSTRIDE = 36;               // floats per lane in the hit staging 
 constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row half
 
 struct Params {
-    const uint8_t *xt;        // bf16 tiles, pre-swizzled (see tile_bf16_kernel)
+    const uint8_t *xt;        // 16-bit tiles, pre-swizzled (see tile_16bit_kernel)
     const float *pnorm;       // [n_pad] f32 squared norms (+inf on padding rows)
     const float *mnorm;       // [n_pad] norms rounded up (0 on padding rows)
     const float *core;        // [n] core distances (Borůvka)
@@ -62,6 +62,10 @@ struct Params {
     uint32_t *cbound;         // Borůvka: per-component upper bound of the cheapest edge (f32 bits)
     int32_t *rowcnt;          // Borůvka: candidates appended per row half ([n][2])
     int cap;                  // Borůvka: candidate slots per row half
+    uint32_t idesc;           // MMA instruction descriptor (bf16 or fp16 operands)
+    float s2, inv_s2;         // operand scale squared (a power of two) and its inverse: the
+                              // screen works in scaled units, inputs and outputs are raw
+    float abs_c;              // absolute error term of the bound (fp16 subnormal rounding)
 };
 
 // ---- PTX wrappers ----
@@ -134,16 +138,17 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
     d |= (uint64_t)2 << 61;            // SWIZZLE_128B
     return d;
 }
-// Instruction descriptor: kind::f16, A/B bf16, D f32, both K-major, M=128, N=256.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptors of kind::f16: D f32, A and B both bf16 (format 1 in bits 7-9 and
+// 10-12) or both fp16 (format 0), both K-major, M=128, N=256.
+constexpr uint32_t IDESC_F16 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t IDESC_BF16 = IDESC_F16 | (1u << 7) | (1u << 10);
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t accumulate) {
+__device__ __forceinline__ void mma_16bit(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate));
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile(
@@ -189,27 +194,34 @@ __host__ __device__ __forceinline__ uint64_t tiled_offset(int64_t r, int f, int 
            (uint64_t)rr * 128 + (uint64_t)chunk * 16 + (uint64_t)(c & 7) * 2;
 }
 
-__global__ void tile_bf16_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
-                                 int64_t n_pad, uint8_t *__restrict__ xt) {
+// 16-bit tiled copy of the (scaled) rows: bf16, or fp16 of x * scale (scale a power of two).
+template <bool FP16>
+__global__ void tile_16bit_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
+                                  int64_t n_pad, float scale, uint8_t *__restrict__ xt) {
     // one thread per (row, group of 8 features): 16 bytes out
     const int groups = d_pad >> 3;
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_pad * groups) return;
     int64_t r = e / groups;
     int g = (int)(e - r * groups);
-    __align__(16) __nv_bfloat16 h[8];
+    __align__(16) uint16_t h[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         int f = g * 8 + q;
         float v = (r < n && f < d) ? x[r * d + f] : 0.0f;
-        h[q] = __float2bfloat16_rn(v);
+        if constexpr (FP16) {
+            h[q] = __half_as_ushort(__float2half_rn(v * scale));
+        } else {
+            h[q] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+        }
     }
     *reinterpret_cast<uint4 *>(xt + tiled_offset(r, g * 8, d_pad)) =
         *reinterpret_cast<const uint4 *>(h);
 }
 
+// Squared norms and rounded-up norms of the scaled rows (x * scale, exact for a power of two).
 __global__ void norms_kernel(const float *__restrict__ x, int64_t n, int d, int64_t n_pad,
-                             float *__restrict__ pnorm, float *__restrict__ mnorm) {
+                             float scale, float *__restrict__ pnorm, float *__restrict__ mnorm) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_pad) return;
     if (r >= n) {
@@ -219,12 +231,24 @@ __global__ void norms_kernel(const float *__restrict__ x, int64_t n, int d, int6
     }
     float acc = 0.0f;
     for (int f = 0; f < d; ++f) {
-        float v = x[r * d + f];
+        float v = x[r * d + f] * scale;
         acc = __fmaf_rn(v, v, acc);
     }
     pnorm[r] = acc;
     // rounded-up norm, widened by 2^-20 so it bounds the true norm despite the f32 sum
     mnorm[r] = __fmul_ru(__fsqrt_ru(acc), 1.0f + 0x1p-20f);
+}
+
+// Largest |x| over all coordinates (non-negative floats order like their bit patterns).
+__global__ void absmax_kernel(const float *__restrict__ x, int64_t count,
+                              unsigned int *__restrict__ out) {
+    float m = 0.0f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
 
 __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t *__restrict__ chunk_lo,
@@ -423,7 +447,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         for (int ks = 0; ks < 4; ++ks) {
                             const uint64_t ad = desc_sw128(a_base + kb * KBLOCK_A + ks * 32);
                             const uint64_t bd = desc_sw128(bstage + kb * KBLOCK_B + ks * 32);
-                            mma_bf16(d_tmem, ad, bd, (kb | ks) != 0);
+                            mma_16bit(d_tmem, ad, bd, P.idesc, (kb | ks) != 0);
                         }
                     }
                     mma_commit(&empty[stage]);
@@ -462,12 +486,12 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             const bool valid = row < P.n;
             const float p_i = valid ? P.pnorm[row] : 0.0f;
             const float m_i = valid ? P.mnorm[row] : 0.0f;
-            const float ps_i = P.one_minus_cb * p_i;
+            const float ps_i = P.one_minus_cb * p_i - P.abs_c;
             const float cm_i = P.c_a * m_i;
             float core_i = 0.0f;
             int32_t lab_i = -1;
             if (BORUVKA && valid) {
-                core_i = P.core[row];
+                core_i = P.core[row] * P.s2;
                 lab_i = P.label[row];
             }
             // kNN: the row's M smallest lower bounds. Borůvka: an upper bound U on the row's
@@ -510,10 +534,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         pre_c.z = col + 2 < P.n ? P.core[col + 2] : 0.0f;
                         pre_c.w = col + 3 < P.n ? P.core[col + 3] : 0.0f;
                     }
+                    pre_c.x *= P.s2;
+                    pre_c.y *= P.s2;
+                    pre_c.z *= P.s2;
+                    pre_c.w *= P.s2;
                     const int64_t ch = t * 8 + half * 4 + (lane & 3);
                     pre_ch = -2;
                     if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
-                    pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i]) : CUSCAN_INF;
+                    pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i]) * P.s2
+                                   : CUSCAN_INF;
                 }
             };
             int64_t ti = next_index(0);
@@ -654,7 +683,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                                     if (cnt < P.cap) P.cand_ids[(row * 2 + half) * P.cap + cnt] = (int32_t)j;
                                     ++cnt;
                                     // upper bound of this pair's weight: D + eps = L + 2 eps
-                                    const float eps2 = 2.0f * fmaf(cm_i, mb[col], P.c_b * (ps_i + pb[col]) * 1.001f);
+                                    const float eps2 =
+                                        2.0f * fmaf(cm_i, mb[col], P.c_b * (ps_i + pb[col]) * 1.001f) +
+                                        4.0f * P.abs_c;
                                     const float ubr = lb + eps2;
                                     const float ub = fmaxf(fmaxf(ubr + 0x1p-20f * (fabsf(ubr) + eps2), core_i), cj);
                                     U = fminf(U, ub);
@@ -673,7 +704,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&t_empty[b]);
                 if (BORUVKA && valid && U < published) {
-                    atomicMin(&P.cbound[lab_i], __float_as_uint(U));
+                    // raw units, rounded up so that the bound stays an upper bound
+                    atomicMin(&P.cbound[lab_i], __float_as_uint(__fmul_ru(U, P.inv_s2)));
                     published = U;
                 }
                 ++tcount;
@@ -688,7 +720,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
 #pragma unroll
                 for (int s2 = 0; s2 < LM; ++s2) {
                     P.cand_ids[base_at + s2] = J[s2];
-                    P.cand_lb[base_at + s2] = L[s2];
+                    // raw units, rounded down so that the bound stays a lower bound
+                    P.cand_lb[base_at + s2] = __fmul_rd(L[s2], P.inv_s2);
                 }
             }
         }
@@ -868,11 +901,16 @@ __global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
     if (i < n) p[i] = v;
 }
 
-// Error bound coefficients for d features (K = padded depth of the bf16 dot product).
-void error_coefficients(int d, int d_pad, float &c_a, float &c_b) {
-    const double u = std::ldexp(1.0, -8);    // bf16 unit roundoff (round to nearest)
-    const double u32 = std::ldexp(1.0, -24); // f32 unit roundoff
-    // bf16 rounding of both factors, plus a generous bound on the tensor-core f32 accumulation
+// Error bound coefficients for d features (K = padded depth of the 16-bit dot product).
+// bf16: unit roundoff 2^-8 over the whole f32 range. fp16: unit roundoff 2^-11 for the scaled
+// values (|x * scale| <= 2^15, so nothing overflows); scaled values below 2^-14 round in the
+// subnormal range with an absolute error of at most 2^-25, which adds at most
+// 2 * [2^-25 (1 + u) sqrt(d) (m_i + m_j) + d 2^-50] to the distance; with every scaled norm at
+// most sqrt(d) 2^15 this is bounded by the constant abs_c.
+void error_coefficients(int d, int d_pad, bool fp16, float &c_a, float &c_b, float &abs_c) {
+    const double u = std::ldexp(1.0, fp16 ? -11 : -8);  // unit roundoff (round to nearest)
+    const double u32 = std::ldexp(1.0, -24);            // f32 unit roundoff
+    // rounding of both factors, plus a generous bound on the tensor-core f32 accumulation
     // (each of K partial sums off by at most 2^-21 of the running magnitude)
     const double a1 = (2.0 * u + u * u) + (double)d_pad * std::ldexp(1.0, -21) * (1 + u) * (1 + u);
     // norms and the reference sum each carry at most (d + 2) f32 roundings; the epilogue adds a
@@ -880,6 +918,25 @@ void error_coefficients(int d, int d_pad, float &c_a, float &c_b) {
     const double b = 3.5 * (double)(d + 4) * u32 + 1e-7;
     c_a = (float)(2.0 * a1 * (1.0 + 1e-4));
     c_b = (float)b;
+    abs_c = 0.0f;
+    if (fp16) {
+        const double eta = std::ldexp(1.0, -25);
+        const double m_max = std::sqrt((double)d) * std::ldexp(1.0, 15);
+        abs_c = (float)(2.0 * (eta * (1 + u) * std::sqrt((double)d) * 2.0 * m_max +
+                               (double)d * eta * eta) * 1.01);
+    }
+}
+
+// Power-of-two scale that brings the largest |x| into [2^14, 2^15) for fp16 operands; 0 when
+// no such scale keeps scale^2 and the scaled sums inside the f32 range (bf16 is used then).
+float fp16_scale(float absmax) {
+    if (absmax == 0.0f) return 1.0f;
+    if (!(absmax > 0.0f) || !std::isfinite(absmax)) return 0.0f;
+    int e = 0;
+    std::frexp((double)absmax, &e);  // absmax in [2^(e-1), 2^e)
+    const int k = 15 - e;            // absmax * 2^k in [2^14, 2^15)
+    if (k > 60 || k < -60) return 0.0f;
+    return (float)std::ldexp(1.0, k);
 }
 
 }  // namespace
@@ -915,6 +972,19 @@ static bool refined_shape_ok(int64_t n, int d, int k) {
     return n >= 2048 && k <= 32 && refined_layout(n, d, L);
 }
 
+size_t refined_workspace_bytes(int64_t n, int d, int k) {
+    Layout L;
+    if (!refined_shape_ok(n, d, k) || !refined_layout(n, d, L)) return 0;
+    constexpr size_t M = 32;
+    size_t b = (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;  // xt, norms
+    b += 3 * sizeof(float) * (size_t)L.n_tiles + 48;          // tile stats, flags, range
+    b += sizeof(int32_t) * (size_t)n;                                                 // fallback
+    b += 2 * 4 * (size_t)n * 2 * M;                  // candidate ids and bounds (two lists of M)
+    b += sizeof(uint32_t) * (size_t)n + 2 * sizeof(int32_t) * (size_t)n;  // cbound, rowcnt
+    b += 256 * sizeof(float) * (size_t)d + 8 * (size_t)n;                 // pivots, cells
+    return b;
+}
+
 static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float *x, int64_t n,
                 int d, const int32_t *chunk_lo, const int32_t *chunk_hi, cudaStream_t s) {
     int rc = ensure(ctx, R.xt, (size_t)L.n_pad * L.d_pad * 2, "bf16 tiles");
@@ -928,14 +998,50 @@ static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float
     if (!rc) rc = ensure(ctx, R.fallback, sizeof(int32_t) * n, "fallback rows");
     if (rc) return rc;
     const int64_t groups = L.n_pad * (L.d_pad / 8);
-    CUSCAN_KERNEL(tile_bf16_kernel, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d, L.d_pad,
-                  L.n_pad, as<uint8_t>(R.xt));
+    if (R.fp16)
+        CUSCAN_KERNEL(tile_16bit_kernel<true>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d,
+                      L.d_pad, L.n_pad, R.scale, as<uint8_t>(R.xt));
+    else
+        CUSCAN_KERNEL(tile_16bit_kernel<false>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n,
+                      d, L.d_pad, L.n_pad, 1.0f, as<uint8_t>(R.xt));
     CUSCAN_KERNEL(norms_kernel, (unsigned)ceil_div(L.n_pad, 256), 256, 0, s, x, n, d, L.n_pad,
-                  as<float>(R.pnorm), as<float>(R.mnorm));
+                  R.fp16 ? R.scale : 1.0f, as<float>(R.pnorm), as<float>(R.mnorm));
     CUSCAN_KERNEL(tile_stats_kernel, (unsigned)ceil_div(L.n_tiles, 128), 128, 0, s,
                   as<float>(R.mnorm), chunk_lo, chunk_hi, L.n_tiles, ceil_div(n, 32),
                   as<float>(R.tile_mmax), as<int32_t>(R.tile_lo), as<int32_t>(R.tile_hi));
     CUSCAN_LAUNCH(ctx, "refined prep");
+    return CUSCAN_OK;
+}
+
+// Operand format of this fit's screens: fp16 of x * scale when the caller asked for it and the
+// data's range admits a power-of-two scale, else bf16. One reduction and one host read per fit.
+static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, int64_t n, int d,
+                           cudaStream_t s) {
+    if (R.have_scale) return CUSCAN_OK;
+    R.fp16 = false;
+    R.scale = 1.0f;
+    if (R.want_fp16) {
+        int rc = ensure(ctx, R.absmax, 16, "range reduction");
+        if (rc) return rc;
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.absmax.ptr, 0, sizeof(unsigned int), s));
+        const int64_t count = n * (int64_t)d;
+        int64_t blocks = ceil_div(count, 256);
+        if (blocks > 8 * (int64_t)ctx->sm_count) blocks = 8 * (int64_t)ctx->sm_count;
+        CUSCAN_KERNEL(absmax_kernel, (unsigned)blocks, 256, 0, s, x, count,
+                      as<unsigned int>(R.absmax));
+        CUSCAN_LAUNCH(ctx, "absmax_kernel");
+        unsigned int bits = 0;
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(&bits, R.absmax.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
+        CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+        float amax;
+        memcpy(&amax, &bits, sizeof(amax));
+        const float sc = fp16_scale(amax);
+        if (sc > 0.0f) {
+            R.fp16 = true;
+            R.scale = sc;
+        }
+    }
+    R.have_scale = true;
     return CUSCAN_OK;
 }
 
@@ -963,10 +1069,15 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.n_chunks = ceil_div(n, 32);
     P.kblocks = L.kblocks;
     P.stages = L.stages;
-    float ca, cb;
-    error_coefficients(d, L.d_pad, ca, cb);
+    float ca, cb, abs_c;
+    error_coefficients(d, L.d_pad, R.fp16, ca, cb, abs_c);
     P.c_a = ca;
     P.one_minus_cb = 1.0f - cb;
+    P.abs_c = abs_c;
+    P.idesc = R.fp16 ? IDESC_F16 : IDESC_BF16;
+    const float sc = R.fp16 ? R.scale : 1.0f;
+    P.s2 = sc * sc;
+    P.inv_s2 = 1.0f / (sc * sc);
     P.cand_ids = as<int32_t>(R.cand_ids);
     P.cand_lb = as<float>(R.cand_lb);
     P.error = as<int>(R.error);
@@ -983,8 +1094,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     }
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
     auto kernel = screen_kernel<M, BORUVKA>;
-    CUSCAN_CUDA(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)L.smem));
+    if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
     int64_t grid = L.n_qblocks < ctx->sm_count ? L.n_qblocks : ctx->sm_count;
     CUSCAN_KERNEL(kernel, (unsigned)grid, THREADS, L.smem, s, P);
     CUSCAN_LAUNCH(ctx, "screen_kernel");
@@ -1014,9 +1124,11 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     RefinedBuffers &R = b.refined;
     Layout L;
     refined_layout(n, d, L);
+    int rc = choose_operands(ctx, R, x, n, d, s);
+    if (rc) return rc;
     // 1. cells: nearest of npiv evenly spaced pivot rows (exact f32, k = 1)
     const int npiv = (int)(n / 256 < 256 ? (n / 256 < 1 ? 1 : n / 256) : 256);
-    int rc = ensure(ctx, R.pivots, sizeof(float) * npiv * d, "cell pivots");
+    rc = ensure(ctx, R.pivots, sizeof(float) * npiv * d, "cell pivots");
     if (!rc) rc = ensure(ctx, R.cells, sizeof(int32_t) * n, "cells");
     if (!rc) rc = ensure(ctx, R.cell_d, sizeof(float) * n, "cell distances");
     if (rc) return rc;
@@ -1067,7 +1179,8 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     RefinedBuffers &R = b.refined;
     Layout L;
     refined_layout(n, d, L);
-    int rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
+    int rc = choose_operands(ctx, R, xp, n, d, s);
+    if (!rc) rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
     if (!rc) rc = prep(ctx, R, L, xp, n, d, clo, chi, s);
     if (rc) return rc;
     // component bounds: +inf, then the exact cross-component edges of the kNN rows
@@ -1099,6 +1212,9 @@ int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t
     if (!refined_layout(n, d, L))
         return fail(ctx, CUSCAN_CAPACITY, "shape outside the tensor-core tiling");
     RefinedBuffers &R = b.refined;
+    R.fp16 = false;  // the raw accumulator of bf16 operands
+    R.scale = 1.0f;
+    R.have_scale = false;
     int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
     if (!rc) rc = run_screen<32, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
     if (rc) return rc;

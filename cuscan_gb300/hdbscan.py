@@ -14,8 +14,9 @@ Differences from the reference, by design:
  * ``backend`` may be "auto" or "cuda"; both run on the GPU. "cpu" raises: this library ships
    no CPU implementation and never falls back to one.
  * ``precision`` selects the distance arithmetic: "fp32" (exact f32 direct differences) or
-   "bf16_refined" (bf16 tensor-core screening with exact f32 re-evaluation); both give
-   bit-identical results.
+   "bf16_refined" (bf16 tensor-core screening with exact f32 re-evaluation) or "fp16_refined"
+   (the same screening with power-of-two-scaled fp16 operands, whose tighter error bound
+   leaves fewer pairs to re-evaluate); all give bit-identical results.
  * ``approximate_predict`` and predictors are not part of this build.
 """
 from __future__ import annotations
@@ -211,8 +212,8 @@ class HDBSCAN:
                 or not isinstance(self.memory_limit_bytes, (int, np.integer))
                 or not 0 < int(self.memory_limit_bytes) <= 2**64 - 1):
             raise ValueError("memory_limit_bytes must be a positive uint64 integer or None")
-        if self.precision not in ("fp32", "bf16_refined"):
-            raise ValueError("precision must be 'fp32' or 'bf16_refined'")
+        if self.precision not in _lib.PRECISIONS:
+            raise ValueError("precision must be 'fp32', 'bf16_refined' or 'fp16_refined'")
         unsupported = (("semi_supervised", self.semi_supervised, False),
                        ("ss_algorithm", self.ss_algorithm, "bc"),
                        ("metric", self.metric, "euclidean"),
@@ -307,7 +308,7 @@ def fit_hdbscan(x: np.ndarray, finite_rows: np.ndarray, *, min_cluster_size: int
     stats = {}
     if n > 1:
         ctx = context(device_index)
-        prec = _lib.PRECISION_BF16_REFINED if precision == "bf16_refined" else _lib.PRECISION_PLAIN
+        prec = _lib.PRECISIONS[precision]
         core = ctx.fit_core(xf, ms, prec)
         stats = core["stats"]
         k = core["knn_ids"].shape[1]

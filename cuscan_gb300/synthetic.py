@@ -78,6 +78,35 @@ def vmf_like(n: int = 500_000, d: int = 128, clusters: int = 100, noise_fraction
     return out[rng.permutation(n)]
 
 
+def gaussian_mixture(n: int, d: int, blobs: int, std_range=(0.5, 2.0), seed: int = 0) -> np.ndarray:
+    """Isotropic Gaussian blobs with centres uniform in [-10, 10]^d, equal weights and a
+    standard deviation per blob uniform in std_range; float32 rows in shuffled order."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-10.0, 10.0, size=(blobs, d))
+    std = rng.uniform(std_range[0], std_range[1], size=blobs)
+    assign = rng.integers(0, blobs, size=n)
+    x = (c[assign] + rng.normal(size=(n, d)) * std[assign, None]).astype(np.float32)
+    return x
+
+
+def fit_request_stream(count: int, seed: int = 46) -> list[dict]:
+    """Specifications of a stream of fit requests: n log-uniform in [500, 50000], d drawn from
+    {16, 32, 64, 128}, a Gaussian mixture of blobs ~ U{2..30} (std U[0.5, 2], centres
+    U[-10, 10]^d); min_samples = 5, min_cluster_size = max(5, n / 200)."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(500), np.log(50000), size=count)).astype(np.int64)
+    d = rng.choice([16, 32, 64, 128], size=count)
+    blobs = rng.integers(2, 31, size=count)
+    return [{"n": int(n[i]), "d": int(d[i]), "blobs": int(blobs[i]), "min_samples": 5,
+             "min_cluster_size": max(5, int(n[i]) // 200), "seed": seed * 1_000_003 + i}
+            for i in range(count)]
+
+
+def request_points(spec: dict) -> np.ndarray:
+    """The point set of one request specification."""
+    return gaussian_mixture(spec["n"], spec["d"], spec["blobs"], seed=spec["seed"])
+
+
 WORKLOADS = {
     # name: (generator, kwargs, min_samples, min_cluster_size)
     "blobs_2k_d10": (blobs_with_noise, dict(n=2000, d=10, seed=42), 5, 5),

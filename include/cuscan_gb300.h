@@ -48,16 +48,23 @@ typedef enum cuscan_status {
     CUSCAN_NUMERICAL = 4,           /* HdbscanError::Numerical */
     CUSCAN_OVERFLOW = 5,            /* HdbscanError::Overflow */
     CUSCAN_CAPACITY = 6,            /* HdbscanError::Capacity */
-    CUSCAN_MEMORY = 7               /* HdbscanError::Memory */
+    CUSCAN_MEMORY = 7,              /* HdbscanError::Memory */
+    CUSCAN_PENDING = 8              /* not an error: a server request is still queued or
+                                       running (returned only by the cuscan_server_* calls) */
 } cuscan_status;
 
-/* Arithmetic used by the distance sweeps of cuscan_fit_core. Both give bit-identical results:
+/* Arithmetic used by the distance sweeps of cuscan_fit_core. All give bit-identical results:
  * PLAIN evaluates every pair with exact f32 direct differences on the SIMT cores;
- * BF16_REFINED screens pairs with bf16 tensor-core GEMM tiles and re-evaluates every pair that
- * the proven error bound cannot rule out with the same exact f32 direct differences. */
+ * BF16_REFINED screens pairs with bf16 tensor-core GEMM tiles (f32 accumulation) and
+ * re-evaluates every pair that the proven error bound cannot rule out with the same exact f32
+ * direct differences; FP16_REFINED does the same with fp16 operands of x * 2^k (k chosen from
+ * the data's largest |x|), whose 8x smaller rounding error leaves fewer pairs to re-evaluate on
+ * data whose norms are large against the neighbour distances (falls back to bf16 operands when
+ * no such scale exists). */
 typedef enum cuscan_precision {
     CUSCAN_PRECISION_PLAIN = 0,
-    CUSCAN_PRECISION_BF16_REFINED = 1
+    CUSCAN_PRECISION_BF16_REFINED = 1,
+    CUSCAN_PRECISION_FP16_REFINED = 2
 } cuscan_precision;
 
 typedef struct cuscan_ctx cuscan_ctx;
@@ -228,6 +235,97 @@ void cuscan_clustering_free(cuscan_clustering *r);
  */
 int cuscan_dbscan_cut(const double *linkage, int64_t rows, double cut, int64_t min_size,
                       int32_t *labels_out);
+
+/* ---------------------------------------------------------------------------------------
+ * Workspace accounting. No reference counterpart: the reference allocates through Burn's
+ * memory pool. These let a caller budget device memory around the fit core.
+ * ------------------------------------------------------------------------------------- */
+
+/* Upper bound on the device workspace cuscan_fit_core allocates for one fit of n rows. */
+int64_t cuscan_fit_workspace_bytes(int64_t n, int32_t d, int32_t min_samples, int32_t precision);
+/* Device bytes the context's workspace holds now (buffers are kept between calls). */
+int64_t cuscan_ctx_reserved_bytes(const cuscan_ctx *ctx);
+/* Synchronise the context's stream and free its workspace. */
+int cuscan_ctx_release_workspace(cuscan_ctx *ctx);
+
+/* ---------------------------------------------------------------------------------------
+ * Fit-request server: continuous batching of HDBSCAN fits on one GPU. No reference
+ * counterpart (the reference fits one point set per call); each request runs the estimator
+ * flow of crates/hdbscan/src/estimator.rs:1034-1392: finite split, cuscan_fit_core, then
+ * cuscan_clusters_from_spanning_tree.
+ *
+ * Requests queue in arrival order and are admitted onto `slots` execution slots, each with its
+ * own CUDA stream, workspace and host thread, as slots and device memory free up: the sum over
+ * slots of max(workspace held, cuscan_fit_workspace_bytes of the running request) stays
+ * within `budget_bytes`. Idle slots release retained workspace when the head request needs
+ * the room; a request whose own bound exceeds the budget finishes at once with CUSCAN_MEMORY.
+ * The fits of different slots overlap on the device. A request's result equals that of the
+ * same fit run alone.
+ *
+ * The caller keeps `data` valid and unchanged until the request has finished. Results stay on
+ * the server until cuscan_server_release. All calls are thread safe.
+ * ------------------------------------------------------------------------------------- */
+typedef struct cuscan_server cuscan_server;
+
+typedef struct cuscan_server_info {
+    int64_t request_id;
+    int32_t status;          /* outcome once finished; CUSCAN_PENDING while queued or running */
+    int32_t slot;            /* slot that ran it, -1 before admission */
+    int64_t n;
+    int64_t finite_rows;
+    int32_t d;
+    int32_t n_clusters;
+    int64_t workspace_bound_bytes;
+    double submit_ms;        /* since the server was created */
+    double queued_ms;        /* submit -> admission */
+    double run_ms;           /* admission -> result ready on the host */
+    double latency_ms;       /* submit -> result ready on the host */
+    double done_ms;          /* since the server was created */
+    double prep_ms;          /* host: finite split and compaction */
+    double fit_ms;           /* host wall time of cuscan_fit_core (copies included) */
+    double extract_ms;       /* host: cuscan_clusters_from_spanning_tree and scatter */
+    cuscan_fit_stats stats;
+} cuscan_server_info;
+
+typedef struct cuscan_server_stats {
+    int32_t slots;
+    int32_t pad;
+    int64_t budget_bytes;
+    int64_t submitted, completed, failed, queued, running;
+    int64_t committed_bytes;       /* current sum of slot commitments */
+    int64_t peak_committed_bytes;  /* largest sum at any admission */
+    int64_t workspace_releases;    /* idle-slot releases ordered by admission */
+} cuscan_server_stats;
+
+int cuscan_server_create(int device, int32_t slots, int64_t budget_bytes, cuscan_server **out,
+                         char *err, size_t err_len);
+/* Scheduling test double: the same queue and admission, with slots that run no fit (each
+ * request waits us_per_kpoint microseconds per 1000 rows and reports its workspace bound as
+ * held). It needs no GPU; cuscan_server_read_fit on it fails. */
+int cuscan_server_create_simulated(int32_t slots, int64_t budget_bytes, double us_per_kpoint,
+                                   cuscan_server **out, char *err, size_t err_len);
+/* Fails queued requests, waits for running ones, stops the slots and frees everything. */
+void cuscan_server_destroy(cuscan_server *server);
+int cuscan_server_submit_fit(cuscan_server *server, const float *data, int64_t n, int32_t d,
+                             int32_t min_samples, int32_t precision,
+                             const cuscan_extract_config *config, int64_t *request_id);
+/* Wait up to timeout_ms (< 0: no limit) for one request; CUSCAN_OK once it has finished
+ * (info->status is its outcome), CUSCAN_PENDING if it has not. */
+int cuscan_server_wait(cuscan_server *server, int64_t request_id, double timeout_ms,
+                       cuscan_server_info *info);
+/* Next finished request in completion order (each is returned once, released requests not
+ * at all); CUSCAN_PENDING on timeout. */
+int cuscan_server_wait_any(cuscan_server *server, double timeout_ms, int64_t *request_id);
+/* labels[n] and probabilities[n] over all submitted rows (non-finite rows: -1 and 0),
+ * core_distances[finite_rows] (Euclidean), sorted_mst[(finite_rows - 1) * 3]; any may be
+ * NULL. Returns the request's failure status if it failed. */
+int cuscan_server_read_fit(cuscan_server *server, int64_t request_id, int32_t *labels,
+                           float *probabilities, float *core_distances, double *sorted_mst);
+int cuscan_server_request_error(cuscan_server *server, int64_t request_id, char *buf,
+                                size_t len);
+/* Drop a finished request's results. */
+int cuscan_server_release(cuscan_server *server, int64_t request_id);
+int cuscan_server_get_stats(cuscan_server *server, cuscan_server_stats *out);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,7 @@ from tests.conftest import load_case
 
 pytestmark = pytest.mark.gpu
 
-PRECISIONS = [_lib.PRECISION_PLAIN, _lib.PRECISION_BF16_REFINED]
+PRECISIONS = [_lib.PRECISION_PLAIN, _lib.PRECISION_BF16_REFINED, _lib.PRECISION_FP16_REFINED]
 
 
 def bits(a):

@@ -1,0 +1,173 @@
+"""Fit-request server: admission by memory budget and queue order on the scheduling test double
+(CPU), and on the GPU that every result equals the same fit run alone."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from cuscan_gb300 import _lib, synthetic
+from cuscan_gb300.serving import FitServer
+
+
+def bound(n, d, ms=5, precision=_lib.PRECISION_BF16_REFINED):
+    return _lib.fit_workspace_bytes(n, d, ms, precision)
+
+
+def drain(server, ids, timeout=30.0):
+    infos = {}
+    for rid in ids:
+        info = server.wait(rid, timeout)
+        assert info is not None, f"request {rid} did not finish"
+        infos[rid] = info
+    return infos
+
+
+def test_workspace_bound_grows_with_shape():
+    small, big = bound(1000, 16), bound(50000, 128)
+    assert 0 < small < big
+    assert bound(5000, 64, precision=_lib.PRECISION_PLAIN) < bound(5000, 64)
+    assert _lib.fit_workspace_bytes(1, 4, 5, 0) == 0
+
+
+def test_budget_is_never_exceeded_and_admission_is_fifo():
+    budget = 3 * bound(20000, 64) + (1 << 20)
+    rng = np.random.default_rng(0)
+    shapes = [(int(rng.integers(500, 20000)), int(rng.choice([16, 32, 64]))) for _ in range(40)]
+    with FitServer(slots=4, budget_bytes=budget, simulated_us_per_kpoint=200.0) as srv:
+        ids = [srv.submit(np.zeros((1, d), np.float32).repeat(n, 0), min_cluster_size=5)
+               for n, d in shapes]
+        infos = drain(srv, ids)
+        st = srv.stats()
+    assert st["completed"] == 40 and st["failed"] == 0
+    assert st["peak_committed_bytes"] <= budget
+    admitted = [infos[r]["submit_ms"] + infos[r]["queued_ms"] for r in ids]
+    assert all(b >= a - 1e-6 for a, b in zip(admitted, admitted[1:])), "admission out of order"
+    assert all(infos[r]["status"] == _lib.OK for r in ids)
+    assert {infos[r]["slot"] for r in ids} <= {0, 1, 2, 3}
+
+
+def test_request_larger_than_budget_fails_with_memory_error():
+    with FitServer(slots=2, budget_bytes=bound(2000, 16), simulated_us_per_kpoint=1.0) as srv:
+        rid = srv.submit(np.zeros((100000, 64), np.float32), min_cluster_size=5)
+        with pytest.raises(MemoryError):
+            srv.result(rid, timeout=5.0)
+        ok = srv.submit(np.zeros((1000, 16), np.float32), min_cluster_size=5)
+        info = srv.wait(ok, 5.0)
+        assert info["status"] == _lib.OK
+
+
+def test_idle_workspace_is_released_for_a_large_request():
+    big = bound(40000, 128)
+    budget = big + bound(4000, 64) // 2
+    with FitServer(slots=3, budget_bytes=budget, simulated_us_per_kpoint=50.0) as srv:
+        small = [srv.submit(np.zeros((4000, 64), np.float32), min_cluster_size=5)
+                 for _ in range(6)]
+        drain(srv, small)
+        assert srv.stats()["committed_bytes"] > 0  # idle slots keep their workspace
+        rid = srv.submit(np.zeros((40000, 128), np.float32), min_cluster_size=5)
+        assert srv.wait(rid, 10.0)["status"] == _lib.OK
+        st = srv.stats()
+    assert st["workspace_releases"] >= 1
+    assert st["peak_committed_bytes"] <= budget
+
+
+def test_wait_times_out_and_wait_any_reports_each_request_once():
+    with FitServer(slots=1, budget_bytes=1 << 34, simulated_us_per_kpoint=20000.0) as srv:
+        slow = srv.submit(np.zeros((20000, 4), np.float32), min_cluster_size=2)   # ~0.4 s
+        queued = srv.submit(np.zeros((10, 4), np.float32), min_cluster_size=2)
+        assert srv.wait(queued, 0.01) is None
+        seen = [srv.wait_any(5.0), srv.wait_any(5.0)]
+        assert seen == [slow, queued]
+        assert srv.wait_any(0.01) is None
+        with pytest.raises(ValueError):  # the test double computes no result
+            srv.result(slow)
+        again = srv.submit(np.zeros((10, 4), np.float32), min_cluster_size=2)
+        srv.wait(again, 5.0)
+        srv.release(again)                 # released before wait_any saw it
+        assert srv.wait_any(0.01) is None
+
+
+def test_close_with_queued_requests_returns():
+    srv = FitServer(slots=1, budget_bytes=1 << 34, simulated_us_per_kpoint=5000.0)
+    for _ in range(5):
+        srv.submit(np.zeros((20000, 4), np.float32), min_cluster_size=2)  # 0.1 s each
+    srv.close()
+
+
+def test_invalid_server_and_request_arguments():
+    with pytest.raises(ValueError):
+        FitServer(slots=0, budget_bytes=1 << 30, simulated_us_per_kpoint=1.0)
+    with FitServer(slots=1, budget_bytes=1 << 30, simulated_us_per_kpoint=1.0) as srv:
+        with pytest.raises(ValueError):
+            srv.submit(np.zeros((0, 3), np.float32))
+        with pytest.raises(ValueError):
+            srv.submit(np.zeros((10, 3), np.float32), precision="fp16")
+        with pytest.raises(ValueError):
+            srv.submit(np.zeros((10, 3), np.float32), min_cluster_size=0)
+
+
+# ---------------------------------------------------------------- GPU ----------------------
+
+def request_mix():
+    rng = np.random.default_rng(21)
+    out = []
+    for i, (n, d) in enumerate([(600, 16), (2500, 32), (9000, 64), (4000, 128), (12000, 16),
+                                (3000, 64), (800, 128), (20000, 32)]):
+        x = synthetic.blobs_with_noise(n=n, d=d, centers=int(rng.integers(2, 30)), seed=100 + i)
+        out.append((x, max(5, n // 200), "bf16_refined" if i % 3 else "fp32"))
+    x = synthetic.blobs_with_noise(n=3000, d=16, centers=6, seed=7)
+    x[::97, 3] = np.nan
+    x[5, 0] = np.inf
+    out.append((x, 15, "bf16_refined"))
+    return out
+
+
+@pytest.mark.gpu
+def test_results_in_the_mix_equal_fits_alone():
+    import cuscan_gb300 as cg
+    mix = request_mix()
+    alone = []
+    for x, mcs, prec in mix:
+        m = cg.HDBSCAN(min_cluster_size=mcs, min_samples=5, precision=prec).fit(x)
+        alone.append(m)
+    with FitServer(slots=4, budget_bytes=8 << 30) as srv:
+        ids = [srv.submit(x, min_cluster_size=mcs, min_samples=5, precision=prec)
+               for x, mcs, prec in mix]
+        results = [srv.result(r, timeout=120.0) for r in ids]
+        st = srv.stats()
+    assert st["completed"] == len(mix) and st["failed"] == 0
+    assert max(r["info"]["slot"] for r in results) > 0  # more than one slot was used
+    for m, r in zip(alone, results):
+        np.testing.assert_array_equal(r["labels"], m.labels_)
+        np.testing.assert_array_equal(r["probabilities"].view(np.uint32),
+                                      np.asarray(m.probabilities_, np.float32).view(np.uint32))
+        np.testing.assert_array_equal(r["core_distances"].view(np.uint32),
+                                      np.asarray(m.core_distances_, np.float32).view(np.uint32))
+        np.testing.assert_array_equal(r["minimum_spanning_tree"], m.minimum_spanning_tree_)
+
+
+@pytest.mark.gpu
+def test_results_repeat_across_submissions():
+    x, mcs, _ = request_mix()[2]
+    with FitServer(slots=3, budget_bytes=4 << 30) as srv:
+        ids = [srv.submit(x, min_cluster_size=mcs, min_samples=5) for _ in range(6)]
+        res = [srv.result(r, timeout=120.0) for r in ids]
+    for r in res[1:]:
+        np.testing.assert_array_equal(r["labels"], res[0]["labels"])
+        np.testing.assert_array_equal(r["minimum_spanning_tree"], res[0]["minimum_spanning_tree"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,d,ms,prec", [(500, 16, 5, 0), (3000, 128, 15, 1), (20000, 64, 10, 1),
+                                         (50000, 128, 5, 1), (7000, 32, 40, 0)])
+def test_workspace_bound_covers_a_fit(n, d, ms, prec):
+    ctx = _lib.Context(0)
+    try:
+        x = synthetic.blobs_with_noise(n=n, d=d, seed=n)
+        ctx.fit_core(x, ms, prec)
+        held = ctx.reserved_bytes()
+        assert 0 < held <= _lib.fit_workspace_bytes(n, d, ms, prec)
+        ctx.release_workspace()
+        assert ctx.reserved_bytes() == 0
+    finally:
+        ctx.close()
