@@ -90,6 +90,7 @@ class FitStats(C.Structure):
         ("fallback_rows", C.c_int64),
         ("boruvka_fallback_rows", C.c_int64),
         ("cross_pairs", C.c_double),
+        ("rescreened_rows", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

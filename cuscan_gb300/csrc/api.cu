@@ -20,7 +20,7 @@ struct FitWorkspace {
 int refined_available();
 int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d, int k,
                        int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
-                       int64_t *fallback_rows);
+                       int64_t *fallback_rows, int64_t *rescreened_rows);
 int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
                               const int32_t *knn_ids, const float *knn_sq, int k,
                               const float *core, const int32_t *label, cudaStream_t s,
@@ -261,7 +261,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     const int k = (int)((int64_t)min_samples < n - 1 ? min_samples : n - 1);
     int32_t *label = as<int32_t>(f->label);
     cudaEvent_t *ev = f->ev;
-    int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0;
+    int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0, rescreened_rows = 0;
     b.refined.want_fp16 = precision == CUSCAN_PRECISION_FP16_REFINED;
     b.refined.have_scale = false;
 
@@ -270,7 +270,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     // ---- core_distances: exact kNN sweep (estimator.rs:591-657) + core column ----
     if (refined)
         rc = launch_knn_refined(ctx, b, data, n, d, k, knn_ids, knn_sq, s, &refined_rows,
-                                &fallback_rows);
+                                &fallback_rows, &rescreened_rows);
     else
         rc = launch_exact_knn_fp32(ctx, data, n, data, n, d, k, 1, 0, 1, knn_ids, knn_sq, s,
                                    b.knn_ids_tmp, b.knn_dist_tmp);
@@ -332,6 +332,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->fallback_rows = fallback_rows;
         stats->boruvka_fallback_rows = boruvka_fallback_rows;
         stats->cross_pairs = cross_pairs;
+        stats->rescreened_rows = rescreened_rows;
     }
     return CUSCAN_OK;
 }

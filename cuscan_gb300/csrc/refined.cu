@@ -66,7 +66,20 @@ struct Params {
     float s2, inv_s2;         // operand scale squared (a power of two) and its inverse: the
                               // screen works in scaled units, inputs and outputs are raw
     float abs_c;              // absolute error term of the bound (fp16 subnormal rounding)
+    // query rows (the A operand): the reference set itself, or a gathered subset
+    const uint8_t *xq;        // 16-bit tiles of the query rows, same layout as xt
+    const float *pq, *mq;     // their squared norms and rounded-up norms
+    int64_t nq;               // query rows
+    const int32_t *qpos;      // position of each query row in the reference order (null: same)
+    const float *qthr;        // threshold mode: per-query upper bound of the k-th distance (raw)
 };
+
+// Screen modes: kNN lists, Borůvka thresholds with shared component bounds, kNN thresholds.
+constexpr int MODE_KNN_LIST = 0;
+constexpr int MODE_BORUVKA = 1;
+constexpr int MODE_KNN_THRESHOLD = 2;
+constexpr int KNN_CAP = 128;  // threshold-mode candidate slots per row half
+constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
 // ---- PTX wrappers ----
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -195,20 +208,23 @@ __host__ __device__ __forceinline__ uint64_t tiled_offset(int64_t r, int f, int 
 }
 
 // 16-bit tiled copy of the (scaled) rows: bf16, or fp16 of x * scale (scale a power of two).
+// Row r of the copy is row rowmap[r] of x (r itself when rowmap is null); rows >= n are zero.
 template <bool FP16>
 __global__ void tile_16bit_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
-                                  int64_t n_pad, float scale, uint8_t *__restrict__ xt) {
+                                  int64_t n_pad, float scale, const int32_t *__restrict__ rowmap,
+                                  uint8_t *__restrict__ xt) {
     // one thread per (row, group of 8 features): 16 bytes out
     const int groups = d_pad >> 3;
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_pad * groups) return;
     int64_t r = e / groups;
     int g = (int)(e - r * groups);
+    const int64_t src = r < n ? (rowmap ? (int64_t)rowmap[r] : r) : 0;
     __align__(16) uint16_t h[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         int f = g * 8 + q;
-        float v = (r < n && f < d) ? x[r * d + f] : 0.0f;
+        float v = (r < n && f < d) ? x[src * d + f] : 0.0f;
         if constexpr (FP16) {
             h[q] = __half_as_ushort(__float2half_rn(v * scale));
         } else {
@@ -219,9 +235,11 @@ __global__ void tile_16bit_kernel(const float *__restrict__ x, int64_t n, int d,
         *reinterpret_cast<const uint4 *>(h);
 }
 
-// Squared norms and rounded-up norms of the scaled rows (x * scale, exact for a power of two).
+// Squared norms and rounded-up norms of the scaled rows (x * scale, exact for a power of two);
+// row r is row rowmap[r] of x when rowmap is given.
 __global__ void norms_kernel(const float *__restrict__ x, int64_t n, int d, int64_t n_pad,
-                             float scale, float *__restrict__ pnorm, float *__restrict__ mnorm) {
+                             float scale, const int32_t *__restrict__ rowmap,
+                             float *__restrict__ pnorm, float *__restrict__ mnorm) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_pad) return;
     if (r >= n) {
@@ -229,9 +247,10 @@ __global__ void norms_kernel(const float *__restrict__ x, int64_t n, int d, int6
         mnorm[r] = 0.0f;
         return;
     }
+    const int64_t src = rowmap ? (int64_t)rowmap[r] : r;
     float acc = 0.0f;
     for (int f = 0; f < d; ++f) {
-        float v = x[r * d + f] * scale;
+        float v = x[src * d + f] * scale;
         acc = __fmaf_rn(v, v, acc);
     }
     pnorm[r] = acc;
@@ -276,11 +295,16 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
 // per-row thresholds tighten at once), then every other tile in one global order shared by all
 // CTAs, so that the blocks running at the same time stream the same tiles and share them in L2.
 constexpr int64_t WARM = 4;
-__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t qb, int64_t i) {
+__device__ __forceinline__ int64_t window_start(const Params &P, int64_t qb) {
     const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
-    int64_t a = (qb * BM) / BN - w / 2;
+    const int64_t first = P.qpos ? (int64_t)P.qpos[qb * BM] : qb * BM;
+    int64_t a = first / BN - w / 2;
     if (a < 0) a = 0;
     if (a > P.n_tiles - w) a = P.n_tiles - w;
+    return a;
+}
+__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_t i) {
+    const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
     if (i < w) return a + i;
     const int64_t j = i - w;
     return j < a ? j : j + w;
@@ -321,8 +345,11 @@ __device__ __forceinline__ void list_insert(float (&L)[M], int (&J)[M], float x,
     }
 }
 
-template <int M, bool BORUVKA>
+template <int M, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
+    constexpr bool BORUVKA = MODE == MODE_BORUVKA;
+    constexpr bool THRESH = MODE == MODE_KNN_THRESHOLD;
+    constexpr bool APPEND = BORUVKA || THRESH;  // threshold modes append to per-row buffers
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t a_bytes = (uint32_t)P.kblocks * KBLOCK_A;
@@ -383,14 +410,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 a_issued = 2u | a_phase;
                 a_phase ^= 1;
                 mbar_expect_tx(a_full, a_bytes);
-                const uint8_t *asrc = P.xt + (uint64_t)(qb >> 1) * (uint64_t)b_bytes +
+                const uint8_t *asrc = P.xq + (uint64_t)(qb >> 1) * (uint64_t)b_bytes +
                                       (uint64_t)(qb & 1) * KBLOCK_A;
                 for (int kb = 0; kb < P.kblocks; ++kb)
                     bulk_g2s(sA + kb * KBLOCK_A, asrc + (uint64_t)kb * KBLOCK_B, KBLOCK_A, a_full);
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+                const int64_t wa = window_start(P, qb);
                 for (int64_t i = 0; i < P.n_tiles; ++i) {
-                    const int64_t t = tile_order(P, qb, i);
+                    const int64_t t = tile_order(P, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
                     issued[stage] = 2u | phase;
@@ -431,9 +459,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+                const int64_t wa = window_start(P, qb);
                 bool ok = true;
                 for (int64_t i = 0; i < P.n_tiles; ++i) {
-                    const int64_t t = tile_order(P, qb, i);
+                    const int64_t t = tile_order(P, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                     if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
@@ -482,10 +511,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
         uint32_t tcount = 0;
         for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
-            const int64_t row = qb * BM + row_local;
-            const bool valid = row < P.n;
-            const float p_i = valid ? P.pnorm[row] : 0.0f;
-            const float m_i = valid ? P.mnorm[row] : 0.0f;
+            const int64_t row = qb * BM + row_local;  // query row
+            const bool valid = row < P.nq;
+            const int64_t self = valid && P.qpos ? (int64_t)P.qpos[row] : row;
+            const float p_i = valid ? P.pq[row] : 0.0f;
+            const float m_i = valid ? P.mq[row] : 0.0f;
             const float ps_i = P.one_minus_cb * p_i - P.abs_c;
             const float cm_i = P.c_a * m_i;
             float core_i = 0.0f;
@@ -494,10 +524,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 core_i = P.core[row] * P.s2;
                 lab_i = P.label[row];
             }
+            // kNN threshold mode: a fixed upper bound of the row's k-th distance (scaled); a row
+            // without one overflows its buffer at once and is resolved exactly
+            const float tau = THRESH && valid ? P.qthr[row] * P.s2 : CUSCAN_INF;
+            const bool tau_ok = !THRESH || tau < CUSCAN_INF;
             // kNN: the row's M smallest lower bounds. Borůvka: an upper bound U on the row's
             // cheapest cross-component edge plus the shared bound of its component; pairs whose
             // lower bound does not exceed min(U, component bound) are appended for re-ranking.
-            constexpr int LM = BORUVKA ? 1 : M;
+            // kNN threshold: every pair whose lower bound does not exceed tau is appended.
+            constexpr int LM = APPEND ? 1 : M;
             float L[LM];
             int J[LM];
 #pragma unroll
@@ -509,9 +544,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             int cnt = 0;
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+            const int64_t wa = window_start(P, qb);
             // next visited position i (>= i0) in this block's tile order
             auto next_index = [&](int64_t i) -> int64_t {
-                while (i < P.n_tiles && tile_skipped<BORUVKA>(P, tile_order(P, qb, i), qlo, qhi)) ++i;
+                while (i < P.n_tiles && tile_skipped<BORUVKA>(P, tile_order(P, wa, i), qlo, qhi)) ++i;
                 return i;
             };
             // per-tile column data, fetched one tile ahead
@@ -546,10 +582,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
             };
             int64_t ti = next_index(0);
-            if (ti < P.n_tiles) prefetch(tile_order(P, qb, ti));
+            if (ti < P.n_tiles) prefetch(tile_order(P, wa, ti));
             bool ok = true;
             while (ti < P.n_tiles) {
-                const int64_t t = tile_order(P, qb, ti);
+                const int64_t t = tile_order(P, wa, ti);
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
@@ -566,15 +602,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb;
                 __syncwarp();
-                if (ti_next < P.n_tiles) prefetch(tile_order(P, qb, ti_next));
+                if (ti_next < P.n_tiles) prefetch(tile_order(P, wa, ti_next));
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
                     tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN + half * HALF;
                 // TMEM loads are software pipelined: chunk c+1 is in flight while chunk c is
                 // screened (rA/rB alternate; the loop is unrolled so both stay in registers)
-                // (Borůvka only: the kNN list leaves no room for the second buffer)
-                constexpr bool PIPE = BORUVKA;
+                // (threshold modes only: the kNN list leaves no room for the second buffer)
+                constexpr bool PIPE = APPEND;
                 uint32_t rA[32], rB[PIPE ? 32 : 1];
                 tmem_ld32_issue(taddr, rA);
                 tmem_ld_wait(rA);
@@ -600,7 +636,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         for (int e = 0; e < 32; ++e)
                             P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
                     }
-                    bool active = valid;
+                    bool active = valid && tau_ok;
                     int32_t clo = 0, chi = 0;
                     if (BORUVKA) {
                         clo = __shfl_sync(0xffffffffu, ch_word, c);
@@ -612,7 +648,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     // norm, then widened by a few ulps so that no pair whose exact-path bound
                     // would enter the list is passed over. For Borůvka the core condition
                     // core_j < T rides along as max(F, core_j + (thr2 - T)).
-                    const float T = BORUVKA ? fminf(U, comp_bound) : L[LM - 1];
+                    const float T = BORUVKA ? fminf(U, comp_bound) : THRESH ? tau : L[LM - 1];
                     const float base = T - ps_i + cm_i * mt;
                     const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
                     const float dlt = thr2 - T;
@@ -669,7 +705,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             const int col = c * 32 + e;
                             const int64_t j = t * BN + half * HALF + col;
                             if (j >= P.n) continue;
-                            if (!BORUVKA && j == row) continue;
+                            if (!BORUVKA && j == self) continue;
                             const float dot = my_v[e];
                             // exact lower bound for this pair (per-column norm instead of the
                             // tile maximum); pb holds (1 - C_B) p_j
@@ -689,6 +725,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                                     const float ubr = lb + eps2;
                                     const float ub = fmaxf(fmaxf(ubr + 0x1p-20f * (fabsf(ubr) + eps2), core_i), cj);
                                     U = fminf(U, ub);
+                                }
+                            } else if constexpr (THRESH) {
+                                if (lb <= tau) {
+                                    if (cnt < P.cap) P.cand_ids[(row * 2 + half) * P.cap + cnt] = (int32_t)j;
+                                    ++cnt;
                                 }
                             } else {
                                 if (lb < L[LM - 1]) list_insert<LM>(L, J, lb, (int)j);
@@ -712,9 +753,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 ti = ti_next;
             }
             if (!ok) break;
-            if (BORUVKA) {
+            if (APPEND) {
                 // each half of a row appends into its own slot range [(2 row + half) * cap, +cap)
-                if (valid) P.rowcnt[row * 2 + half] = cnt;
+                if (valid) P.rowcnt[row * 2 + half] = tau_ok ? cnt : P.cap + 1;
             } else if (valid) {
                 const int64_t base_at = row * (2 * M) + half * M;
 #pragma unroll
@@ -774,6 +815,7 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__
                                   int64_t n, int d, int k, const int32_t *__restrict__ cand_ids,
                                   const float *__restrict__ cand_lb, int32_t *__restrict__ ids,
                                   float *__restrict__ dist, int32_t *__restrict__ fallback,
+                                  float *__restrict__ fallback_thr,
                                   int *__restrict__ fallback_count) {
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -817,12 +859,72 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__
             }
         }
     }
-    // every pair outside a full list has a lower bound >= that list's M-th bound
+    // every pair outside a full list has a lower bound >= that list's M-th bound; an
+    // inconclusive row is listed by position with dk, an upper bound of its k-th distance
     const float bound = unseen_bound<M>(cand_ids + row * W, cand_lb + row * W);
     if (lane == 0 && !(bound > dk)) {
         const int at = atomicAdd(fallback_count, 1);
-        fallback[at] = (int32_t)orow;
+        fallback[at] = (int32_t)row;
+        fallback_thr[at] = dk;
     }
+}
+
+// kNN re-rank of the threshold screen: query q (position qpos[q]) holds every pair whose lower
+// bound does not exceed an upper bound of its k-th distance, so the exact top k of its appended
+// candidates by (d, original id) is its exact kNN row. A buffer that overflowed (or a row with
+// fewer than k candidates) sends the row's original index to the exact f32 sweep.
+__global__ void rerank_knn_threshold_kernel(const float *__restrict__ x,
+                                            const int32_t *__restrict__ perm,
+                                            const int32_t *__restrict__ qpos, int64_t nq, int d,
+                                            int k, const int32_t *__restrict__ cand_ids,
+                                            const int32_t *__restrict__ rowcnt, int cap,
+                                            int32_t *__restrict__ ids, float *__restrict__ dist,
+                                            int32_t *__restrict__ fallback,
+                                            int *__restrict__ fallback_count) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= nq) return;
+    constexpr int PER = 2 * KNN_CAP / 32;
+    const int64_t pos = qpos[q];
+    const int64_t orow = perm[pos];
+    const int c0 = rowcnt[q * 2], c1 = rowcnt[q * 2 + 1];
+    if (c0 > cap || c1 > cap || c0 + c1 < k) {
+        if (lane == 0) fallback[atomicAdd(fallback_count, 1)] = (int32_t)orow;
+        return;
+    }
+    const float *xr = x + pos * d;
+    unsigned long long key[PER];
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const int s = lane + 32 * t;
+        key[t] = ~0ull;
+        if (s < c0 + c1) {
+            const int32_t j = s < c0 ? cand_ids[(q * 2) * cap + s]
+                                     : cand_ids[(q * 2 + 1) * cap + (s - c0)];
+            const float dd = exact_d2(xr, x + (int64_t)j * d, d);
+            key[t] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
+        }
+    }
+    for (int r = 0; r < k; ++r) {
+        unsigned long long mine = key[0];
+#pragma unroll
+        for (int t = 1; t < PER; ++t) mine = key[t] < mine ? key[t] : mine;
+        const unsigned long long best = warp_min_u64(mine);
+#pragma unroll
+        for (int t = 0; t < PER; ++t)
+            if (key[t] == best) key[t] = ~0ull;
+        if (lane == 0) {
+            ids[orow * k + r] = (int32_t)(uint32_t)best;
+            dist[orow * k + r] = __uint_as_float((uint32_t)(best >> 32));
+        }
+    }
+}
+
+// Original row of each listed position (in place).
+__global__ void positions_to_rows_kernel(int32_t *__restrict__ list, int64_t count,
+                                         const int32_t *__restrict__ perm) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) list[i] = perm[list[i]];
 }
 
 // Borůvka re-rank over component-sorted positions: exact weight of every appended candidate of
@@ -982,7 +1084,28 @@ size_t refined_workspace_bytes(int64_t n, int d, int k) {
     b += 2 * 4 * (size_t)n * 2 * M;                  // candidate ids and bounds (two lists of M)
     b += sizeof(uint32_t) * (size_t)n + 2 * sizeof(int32_t) * (size_t)n;  // cbound, rowcnt
     b += 256 * sizeof(float) * (size_t)d + 8 * (size_t)n;                 // pivots, cells
+    // threshold re-screen of inconclusive kNN rows (at most all n): thresholds, tiles, norms,
+    // candidates, counts, fallback list
+    b += 4 * (size_t)n + (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;
+    b += 4 * (size_t)n * 2 * KNN_CAP + 8 * (size_t)n + 4 * (size_t)n;
     return b;
+}
+
+// 16-bit tiled copy and norms of n rows (row r = rowmap[r] of x, or r), padded to n_pad rows.
+static int tile_rows(cuscan_ctx *ctx, const RefinedBuffers &R, const float *x, int64_t n, int d,
+                     int d_pad, int64_t n_pad, const int32_t *rowmap, uint8_t *xt, float *pnorm,
+                     float *mnorm, cudaStream_t s) {
+    const int64_t groups = n_pad * (d_pad / 8);
+    if (R.fp16)
+        CUSCAN_KERNEL(tile_16bit_kernel<true>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d,
+                      d_pad, n_pad, R.scale, rowmap, xt);
+    else
+        CUSCAN_KERNEL(tile_16bit_kernel<false>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n,
+                      d, d_pad, n_pad, 1.0f, rowmap, xt);
+    CUSCAN_KERNEL(norms_kernel, (unsigned)ceil_div(n_pad, 256), 256, 0, s, x, n, d, n_pad,
+                  R.fp16 ? R.scale : 1.0f, rowmap, pnorm, mnorm);
+    CUSCAN_LAUNCH(ctx, "16-bit tiles");
+    return CUSCAN_OK;
 }
 
 static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float *x, int64_t n,
@@ -996,16 +1119,11 @@ static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float
     if (!rc) rc = ensure(ctx, R.error, 16, "error flag");
     if (!rc) rc = ensure(ctx, R.count, 16, "fallback count");
     if (!rc) rc = ensure(ctx, R.fallback, sizeof(int32_t) * n, "fallback rows");
+    if (!rc) rc = ensure(ctx, R.qthr, sizeof(float) * n, "fallback thresholds");
     if (rc) return rc;
-    const int64_t groups = L.n_pad * (L.d_pad / 8);
-    if (R.fp16)
-        CUSCAN_KERNEL(tile_16bit_kernel<true>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d,
-                      L.d_pad, L.n_pad, R.scale, as<uint8_t>(R.xt));
-    else
-        CUSCAN_KERNEL(tile_16bit_kernel<false>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n,
-                      d, L.d_pad, L.n_pad, 1.0f, as<uint8_t>(R.xt));
-    CUSCAN_KERNEL(norms_kernel, (unsigned)ceil_div(L.n_pad, 256), 256, 0, s, x, n, d, L.n_pad,
-                  R.fp16 ? R.scale : 1.0f, as<float>(R.pnorm), as<float>(R.mnorm));
+    if ((rc = tile_rows(ctx, R, x, n, d, L.d_pad, L.n_pad, nullptr, as<uint8_t>(R.xt),
+                        as<float>(R.pnorm), as<float>(R.mnorm), s)))
+        return rc;
     CUSCAN_KERNEL(tile_stats_kernel, (unsigned)ceil_div(L.n_tiles, 128), 128, 0, s,
                   as<float>(R.mnorm), chunk_lo, chunk_hi, L.n_tiles, ceil_div(n, 32),
                   as<float>(R.tile_mmax), as<int32_t>(R.tile_lo), as<int32_t>(R.tile_hi));
@@ -1045,10 +1163,24 @@ static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, i
     return CUSCAN_OK;
 }
 
-template <int M, bool BORUVKA>
+// A operand of a screen and the outputs of the kNN threshold mode; the defaults mean the
+// reference rows themselves.
+struct QuerySet {
+    const uint8_t *xq = nullptr;
+    const float *pq = nullptr, *mq = nullptr;
+    int64_t nq = -1;
+    const int32_t *qpos = nullptr;
+    const float *qthr = nullptr;
+    int32_t *cand_ids = nullptr;
+    int32_t *rowcnt = nullptr;
+};
+
+template <int M, int MODE>
 static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64_t n, int d,
                       const float *core, const int32_t *label, const int32_t *chunk_lo,
-                      const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr) {
+                      const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr,
+                      const QuerySet &Q = QuerySet()) {
+    constexpr bool BORUVKA = MODE == MODE_BORUVKA;
     int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * 2 * M, "screen candidates");
     if (!rc) rc = ensure(ctx, R.cand_lb, sizeof(float) * n * 2 * M, "screen bounds");
     if (rc) return rc;
@@ -1056,6 +1188,12 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.xt = as<uint8_t>(R.xt);
     P.pnorm = as<float>(R.pnorm);
     P.mnorm = as<float>(R.mnorm);
+    P.xq = Q.xq ? Q.xq : P.xt;
+    P.pq = Q.pq ? Q.pq : P.pnorm;
+    P.mq = Q.mq ? Q.mq : P.mnorm;
+    P.nq = Q.nq >= 0 ? Q.nq : n;
+    P.qpos = Q.qpos;
+    P.qthr = Q.qthr;
     P.core = core;
     P.label = label;
     P.tile_mmax = as<float>(R.tile_mmax);
@@ -1065,7 +1203,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.tile_hi = as<int32_t>(R.tile_hi);
     P.n = n;
     P.n_tiles = L.n_tiles;
-    P.n_qblocks = L.n_qblocks;
+    P.n_qblocks = ceil_div(P.nq, (int64_t)BM);
     P.n_chunks = ceil_div(n, 32);
     P.kblocks = L.kblocks;
     P.stages = L.stages;
@@ -1092,10 +1230,16 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         P.rowcnt = as<int32_t>(R.rowcnt);
         CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowcnt.ptr, 0, sizeof(int32_t) * 2 * n, s));
     }
+    if (MODE == MODE_KNN_THRESHOLD) {
+        P.cap = KNN_CAP;
+        P.cand_ids = Q.cand_ids;
+        P.rowcnt = Q.rowcnt;
+    }
+    if (P.n_qblocks == 0) return CUSCAN_OK;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
-    auto kernel = screen_kernel<M, BORUVKA>;
+    auto kernel = screen_kernel<M, MODE>;
     if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
-    int64_t grid = L.n_qblocks < ctx->sm_count ? L.n_qblocks : ctx->sm_count;
+    int64_t grid = P.n_qblocks < ctx->sm_count ? P.n_qblocks : ctx->sm_count;
     CUSCAN_KERNEL(kernel, (unsigned)grid, THREADS, L.smem, s, P);
     CUSCAN_LAUNCH(ctx, "screen_kernel");
     return CUSCAN_OK;
@@ -1115,7 +1259,7 @@ static int read_screen_status(cuscan_ctx *ctx, RefinedBuffers &R, cudaStream_t s
 
 int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d, int k,
                        int32_t *ids, float *dist, cudaStream_t s, int64_t *refined_rows,
-                       int64_t *fallback_rows) {
+                       int64_t *fallback_rows, int64_t *rescreened_rows) {
     if (!refined_shape_ok(n, d, k)) {
         // shapes outside the tensor-core tiling run the exact f32 sweep
         return launch_exact_knn_fp32(ctx, x, n, x, n, d, k, 1, 0, 1, ids, dist, s, b.knn_ids_tmp,
@@ -1147,20 +1291,63 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     // 3. screen + exact re-rank in sorted positions, outputs in original rows
     if ((rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s))) return rc;
     constexpr int M = 32;
-    if ((rc = run_screen<M, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
+    if ((rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xs, perm, n, d,
                   k, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
-                  as<int32_t>(R.fallback), as<int>(R.count));
+                  as<int32_t>(R.fallback), as<float>(R.qthr), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
     int fallbacks = 0;
     if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
     if (refined_rows) *refined_rows += n;
-    if (fallback_rows) *fallback_rows += fallbacks;
-    // 4. inconclusive rows (original indices): exact f32 sweep
-    if (fallbacks > 0)
-        return launch_exact_knn_fp32(ctx, x, fallbacks, x, n, d, k, 1, 0, 1, ids, dist, s,
-                                     b.knn_ids_tmp, b.knn_dist_tmp, as<int32_t>(R.fallback));
+    if (fallbacks == 0) return CUSCAN_OK;
+    int32_t *exact_rows = as<int32_t>(R.fallback);
+    int exact = fallbacks;
+    if (fallbacks >= RESCREEN_MIN_ROWS && k <= 2 * KNN_CAP) {
+        // 4. inconclusive rows, screened again in threshold mode: every pair whose bound does
+        // not exceed the row's k-th distance among its candidates is appended and re-ranked
+        const int64_t nq = fallbacks;
+        const int64_t nq_pad = ceil_div(nq, (int64_t)BN) * BN;
+        rc = ensure(ctx, R.xq, (size_t)nq_pad * L.d_pad * 2, "re-screen tiles");
+        if (!rc) rc = ensure(ctx, R.pq, sizeof(float) * nq_pad, "re-screen norms");
+        if (!rc) rc = ensure(ctx, R.mq, sizeof(float) * nq_pad, "re-screen norms");
+        if (!rc) rc = ensure(ctx, R.cand2, sizeof(int32_t) * nq * 2 * KNN_CAP, "re-screen candidates");
+        if (!rc) rc = ensure(ctx, R.rowcnt2, sizeof(int32_t) * nq * 2, "re-screen counts");
+        if (!rc) rc = ensure(ctx, R.fallback2, sizeof(int32_t) * nq, "re-screen fallbacks");
+        if (!rc) rc = tile_rows(ctx, R, xs, nq, d, L.d_pad, nq_pad, as<int32_t>(R.fallback),
+                                as<uint8_t>(R.xq), as<float>(R.pq), as<float>(R.mq), s);
+        if (rc) return rc;
+        QuerySet Q;
+        Q.xq = as<uint8_t>(R.xq);
+        Q.pq = as<float>(R.pq);
+        Q.mq = as<float>(R.mq);
+        Q.nq = nq;
+        Q.qpos = as<int32_t>(R.fallback);
+        Q.qthr = as<float>(R.qthr);
+        Q.cand_ids = as<int32_t>(R.cand2);
+        Q.rowcnt = as<int32_t>(R.rowcnt2);
+        if ((rc = run_screen<M, MODE_KNN_THRESHOLD>(ctx, R, L, n, d, nullptr, nullptr, nullptr,
+                                                   nullptr, s, nullptr, Q)))
+            return rc;
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+        CUSCAN_KERNEL(rerank_knn_threshold_kernel, (unsigned)ceil_div(nq * 32, 256), 256, 0, s, xs,
+                      perm, as<int32_t>(R.fallback), nq, d, k, as<int32_t>(R.cand2),
+                      as<int32_t>(R.rowcnt2), KNN_CAP, ids, dist, as<int32_t>(R.fallback2),
+                      as<int>(R.count));
+        CUSCAN_LAUNCH(ctx, "rerank_knn_threshold_kernel");
+        if ((rc = read_screen_status(ctx, R, s, exact))) return rc;
+        if (rescreened_rows) *rescreened_rows += fallbacks;
+        exact_rows = as<int32_t>(R.fallback2);
+    } else {
+        CUSCAN_KERNEL(positions_to_rows_kernel, (unsigned)ceil_div((int64_t)fallbacks, 256), 256, 0,
+                      s, exact_rows, (int64_t)fallbacks, perm);
+        CUSCAN_LAUNCH(ctx, "positions_to_rows_kernel");
+    }
+    if (fallback_rows) *fallback_rows += exact;
+    // 5. rows still inconclusive (original indices): exact f32 sweep
+    if (exact > 0)
+        return launch_exact_knn_fp32(ctx, x, exact, x, n, d, k, 1, 0, 1, ids, dist, s,
+                                     b.knn_ids_tmp, b.knn_dist_tmp, exact_rows);
     return CUSCAN_OK;
 }
 
@@ -1191,7 +1378,7 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                   core, label, n, as<uint32_t>(R.cbound));
     CUSCAN_LAUNCH(ctx, "component bounds");
     constexpr int M = 32;
-    if ((rc = run_screen<M, true>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
+    if ((rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xp, corep,
                   labp, perm, n, d, as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
@@ -1216,7 +1403,7 @@ int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t
     R.scale = 1.0f;
     R.have_scale = false;
     int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
-    if (!rc) rc = run_screen<32, false>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
+    if (!rc) rc = run_screen<32, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
     if (rc) return rc;
     int fallbacks = 0;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));

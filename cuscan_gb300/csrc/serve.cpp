@@ -423,7 +423,8 @@ int cuscan_server_submit_fit(cuscan_server *s, const float *data, int64_t n, int
     if (n <= 0 || d <= 0 || (!data && !s->simulated)) return CUSCAN_INVALID_INPUT;
     if (n > INT32_MAX - 1) return CUSCAN_OVERFLOW;
     if (min_samples <= 0 || config->min_cluster_size <= 0) return CUSCAN_INVALID_CONFIG;
-    if (precision != CUSCAN_PRECISION_PLAIN && precision != CUSCAN_PRECISION_BF16_REFINED)
+    if (precision != CUSCAN_PRECISION_PLAIN && precision != CUSCAN_PRECISION_BF16_REFINED &&
+        precision != CUSCAN_PRECISION_FP16_REFINED)
         return CUSCAN_INVALID_CONFIG;
     auto r = std::make_unique<Request>();
     r->x = data;

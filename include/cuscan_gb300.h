@@ -79,9 +79,10 @@ typedef struct cuscan_fit_stats {
     int64_t seed_edges;      /* edges added by the kNN seed */
     int64_t components_after_seed;
     int64_t refined_rows;    /* kNN rows screened on the tensor cores */
-    int64_t fallback_rows;   /* kNN rows whose screen was inconclusive and ran exact f32 */
+    int64_t fallback_rows;   /* kNN rows whose screens were inconclusive and ran exact f32 */
     int64_t boruvka_fallback_rows; /* Borůvka rows (summed over rounds) re-run exact f32 */
     double cross_pairs;      /* sum over rounds of ordered cross-component pairs */
+    int64_t rescreened_rows; /* kNN rows screened a second time in threshold mode */
 } cuscan_fit_stats;
 
 /* ---- context ---- */

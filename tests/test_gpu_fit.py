@@ -180,6 +180,18 @@ def test_refined_vmf_matches_oracle_and_uses_tensor_screen(gpu_ctx):
     assert_fit_equal(got, O.fit_core(x, 15))
 
 
+@pytest.mark.parametrize("precision", [_lib.PRECISION_BF16_REFINED, _lib.PRECISION_FP16_REFINED])
+def test_threshold_rescreen_matches_oracle(gpu_ctx, precision):
+    """Gaussian blobs far from the origin (centres in [-10, 10]^64, std 0.5-2): the first kNN
+    screen leaves hundreds of rows inconclusive, which the threshold re-screen resolves; the
+    result equals the oracle bit for bit."""
+    x = synthetic.gaussian_mixture(20000, 64, 25, seed=20064)
+    got = gpu_ctx.fit_core(x, 5, precision)
+    assert got["stats"]["rescreened_rows"] >= 256
+    assert got["stats"]["fallback_rows"] < got["stats"]["rescreened_rows"]
+    assert_fit_equal(got, O.fit_core(x, 5))
+
+
 def test_full_size_refined_equals_plain(gpu_ctx):
     """vmf_500k_d128 reduced to n=120000: bf16-refined and plain fits agree bit for bit."""
     x, ms, _ = synthetic.workload("vmf_500k_d128", n=120000)

@@ -104,6 +104,9 @@ def test_invalid_server_and_request_arguments():
             srv.submit(np.zeros((10, 3), np.float32), precision="fp16")
         with pytest.raises(ValueError):
             srv.submit(np.zeros((10, 3), np.float32), min_cluster_size=0)
+        for prec in ("fp32", "bf16_refined", "fp16_refined"):
+            rid = srv.submit(np.zeros((10, 3), np.float32), precision=prec)
+            assert srv.wait(rid, 5.0)["status"] == _lib.OK
 
 
 # ---------------------------------------------------------------- GPU ----------------------
