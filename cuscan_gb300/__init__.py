@@ -6,7 +6,9 @@ The product is the C-ABI shared library built from ``csrc/`` (declared in
 """
 from ._lib import Context, clusters_from_spanning_tree, dbscan_cut, load, library_path
 from .hdbscan import HDBSCAN, context, fit_hdbscan
+from .prediction import HDBSCANPredictor
+from .serving import FitServer
 
-__all__ = ["HDBSCAN", "Context", "context", "fit_hdbscan", "clusters_from_spanning_tree",
-           "dbscan_cut", "load", "library_path"]
+__all__ = ["HDBSCAN", "HDBSCANPredictor", "FitServer", "Context", "context", "fit_hdbscan",
+           "clusters_from_spanning_tree", "dbscan_cut", "load", "library_path"]
 __version__ = "0.1.0"

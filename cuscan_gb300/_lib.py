@@ -58,6 +58,15 @@ SIGNATURES = {
                                       _F32P]),
     "cuscan_clustering_free": (None, [_VP]),
     "cuscan_dbscan_cut": (C.c_int, [_F64P, C.c_int64, C.c_double, C.c_int64, _I32P]),
+    "cuscan_predictor_create": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, _VP, _VP,
+                                          _VP, _VP, C.c_int64, _VP, C.c_int64, _VP, _VP,
+                                          C.POINTER(_VP), C.c_char_p, C.c_size_t]),
+    "cuscan_predictor_destroy": (None, [_VP]),
+    "cuscan_predictor_no_cluster_tree": (C.c_int, [_VP]),
+    "cuscan_predictor_read_cores": (C.c_int, [_VP, _VP]),
+    "cuscan_predictor_predict": (C.c_int, [_VP, _VP, _VP, C.c_int64, _VP, _VP, _VP]),
+    "cuscan_predictor_predict_candidates": (C.c_int, [_VP, _VP, _VP, C.c_int64, _VP, _VP, _VP,
+                                                      C.c_char_p, C.c_size_t]),
     "cuscan_fit_workspace_bytes": (C.c_int64, [C.c_int64, C.c_int32, C.c_int32, C.c_int32]),
     "cuscan_ctx_reserved_bytes": (C.c_int64, [_VP]),
     "cuscan_ctx_release_workspace": (C.c_int, [_VP]),

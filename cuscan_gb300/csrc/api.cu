@@ -5,16 +5,9 @@
 
 #include "common.cuh"
 #include "forest.cuh"
+#include "workspace.cuh"
 
 namespace cuscan {
-
-struct FitWorkspace {
-    ForestBuffers forest;
-    Buffer x, ids, dsq, core, label, src, dst, w;  // device copies for the host-pointer entry
-    Buffer op_keys, op_tiles_lo, op_tiles_hi, op_partials, op_knn_ids, op_knn_dist;
-    DevStatus *host_status = nullptr;              // pinned
-    cudaEvent_t ev[6] = {};
-};
 
 // Refined (bf16 tensor-core) sweeps; defined in refined.cu.
 int refined_available();
@@ -33,12 +26,14 @@ size_t refined_workspace_bytes(int64_t n, int d, int k);
 static int workspace_buffers(FitWorkspace *f, Buffer **out) {
     Buffer *own[] = {&f->x, &f->ids, &f->dsq, &f->core, &f->label, &f->src, &f->dst, &f->w,
                      &f->op_keys, &f->op_tiles_lo, &f->op_tiles_hi, &f->op_partials,
-                     &f->op_knn_ids, &f->op_knn_dist};
+                     &f->op_knn_ids, &f->op_knn_dist, &f->pred_q, &f->pred_ids,
+                     &f->pred_dist};
     const int n_own = (int)(sizeof(own) / sizeof(own[0]));
+    static_assert(sizeof(own) / sizeof(own[0]) == kOwnBufferCount, "buffer list");
     for (int i = 0; i < n_own; ++i) out[i] = own[i];
     return n_own + forest_buffers(f->forest, out + n_own);
 }
-constexpr int kWorkspaceBufferCount = 14 + kForestBufferCount;
+constexpr int kWorkspaceBufferCount = kOwnBufferCount + kForestBufferCount;
 
 }  // namespace cuscan
 

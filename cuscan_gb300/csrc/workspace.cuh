@@ -1,0 +1,19 @@
+// Per-context device workspace (buffers are kept between calls and grow on demand).
+#pragma once
+
+#include "common.cuh"
+#include "forest.cuh"
+
+namespace cuscan {
+
+struct FitWorkspace {
+    ForestBuffers forest;
+    Buffer x, ids, dsq, core, label, src, dst, w;  // device copies for the host-pointer entry
+    Buffer op_keys, op_tiles_lo, op_tiles_hi, op_partials, op_knn_ids, op_knn_dist;
+    Buffer pred_q, pred_ids, pred_dist;            // approximate_predict queries and candidates
+    DevStatus *host_status = nullptr;              // pinned
+    cudaEvent_t ev[6] = {};
+};
+constexpr int kOwnBufferCount = 17;
+
+}  // namespace cuscan

@@ -17,13 +17,16 @@ Differences from the reference, by design:
    "bf16_refined" (bf16 tensor-core screening with exact f32 re-evaluation) or "fp16_refined"
    (the same screening with power-of-two-scaled fp16 operands, whose tighter error bound
    leaves fewer pairs to re-evaluate); all give bit-identical results.
- * ``approximate_predict`` and predictors are not part of this build.
+ * ``approximate_predict`` runs the exact candidate search on the GPU and the reference's
+   hierarchy math on the host (``cuscan_gb300.prediction``).
 """
 from __future__ import annotations
 
 import numpy as np
 
 from . import _lib
+from .prediction import (HDBSCANPredictor, Predictor, approximate_predict,
+                         prediction_core_from_knn)
 
 _ARRAY_NAMES = (
     "labels", "probabilities", "condensed_tree", "single_linkage_tree",
@@ -285,11 +288,41 @@ class HDBSCAN:
             return np.full(raw_n, -1, np.intp)
         return np.asarray(_lib.dbscan_cut(linkage, float(eps), st["min_samples"]), np.intp)
 
-    def approximate_predict(self, points):
-        raise NotImplementedError("approximate_predict is not part of the cuscan_gb300 fit core")
+    def _predictor(self) -> Predictor:
+        if not hasattr(self, "_fitted_state"):
+            raise ValueError("This HDBSCAN instance is not fitted yet")
+        st = self._fitted_state
+        if st.get("predictor") is None:
+            arrays = st["arrays"]
+            tree = arrays["condensed_tree"]
+            clustered = bool(np.any(np.asarray(tree["child_size"]) > 1))
+            ms = st["min_samples"]
+            n_finite = arrays["finite_index"].shape[0]
+            if clustered and 2 * ms > n_finite:
+                raise ValueError(
+                    f"approximate_predict needs 2*min_samples = {2 * ms} neighbors but the model "
+                    f"has only {n_finite} finite training points")
+            st["predictor"] = Predictor(
+                condensed_tree=tree, labels=arrays["labels"],
+                finite_index=arrays["finite_index"], min_samples=ms,
+                n_features=st["n_features_in"],
+                train=st["fit_rows"] if clustered else None,
+                prediction_core=(st["prediction_core"] if st["prediction_core"] is not None
+                                 else np.zeros(n_finite, np.float64)),
+                context=context(st["device_index"]) if clustered else None)
+        return st["predictor"]
 
-    def to_predictor(self):
-        raise NotImplementedError("predictors are not part of the cuscan_gb300 fit core")
+    def approximate_predict(self, X, return_connecting_points=False):
+        """Predict fitted cluster labels for new points (original hdbscan
+        ``approximate_predict``): ``(labels, strengths)`` or, with
+        ``return_connecting_points=True``, ``(labels, strengths, connecting_points)``."""
+        if not isinstance(return_connecting_points, (bool, np.bool_)):
+            raise ValueError("return_connecting_points must be a boolean")
+        return approximate_predict(self._predictor(), X, return_connecting_points)
+
+    def to_predictor(self) -> HDBSCANPredictor:
+        """Prepare and return a detached prediction-only view of this fitted model."""
+        return HDBSCANPredictor._from_predictor(self._predictor())
 
 
 def fit_hdbscan(x: np.ndarray, finite_rows: np.ndarray, *, min_cluster_size: int,
@@ -311,6 +344,7 @@ def fit_hdbscan(x: np.ndarray, finite_rows: np.ndarray, *, min_cluster_size: int
         prec = _lib.PRECISIONS[precision]
         core = ctx.fit_core(xf, ms, prec)
         stats = core["stats"]
+        prediction_core = (prediction_core_from_knn(core["knn_sq"], ms) if ms <= n else None)
         k = core["knn_ids"].shape[1]
         core_distances = np.sqrt(core["core_sq"]).astype(np.float32)
         if k == ms:
@@ -336,6 +370,7 @@ def fit_hdbscan(x: np.ndarray, finite_rows: np.ndarray, *, min_cluster_size: int
         prob_f = host["probabilities"]
         mst = host["sorted_mst"]
     else:  # one finite row: all noise, empty trees (hdbscan-core lib.rs:40-50)
+        prediction_core = np.zeros(n, np.float64)
         neighbors = np.empty((0, ms), np.intp)
         core_distances = np.full(n, np.inf, np.float32)
         linkage = np.empty((0, 4), np.float64)
@@ -368,4 +403,8 @@ def fit_hdbscan(x: np.ndarray, finite_rows: np.ndarray, *, min_cluster_size: int
         "n_features_in": d,
         "min_samples": ms,
         "stats": stats,
+        # prediction state: finite training rows (compact order) and their prediction cores
+        "fit_rows": np.ascontiguousarray(xf, np.float32),
+        "prediction_core": prediction_core,
+        "device_index": device_index,
     }

@@ -238,6 +238,48 @@ int cuscan_dbscan_cut(const double *linkage, int64_t rows, double cut, int64_t m
                       int32_t *labels_out);
 
 /* ---------------------------------------------------------------------------------------
+ * approximate_predict. A predictor holds the prediction hierarchy of a fitted model
+ * (hdbscan_core::prediction::PredictionHierarchy::new, crates/hdbscan-core/src/prediction.rs:
+ * 433-700), the prediction core distances and a device copy of the finite training rows.
+ * Predictions follow predict_row (prediction.rs:855-925) on exact candidate rows of width
+ * 2 * min_samples (crates/hdbscan/src/prediction.rs:1806-1978).
+ * ------------------------------------------------------------------------------------- */
+typedef struct cuscan_predictor cuscan_predictor;
+
+/*
+ * Build a predictor from a fitted model: the raw-id condensed tree (rows of parent, child,
+ * lambda, child_size), raw fitted labels[raw_n] and the ascending finite_index[n_finite].
+ * train[n_finite * d] (host) are the finite training rows in compact order; they are copied to
+ * the context's device. prediction_core[n_finite] (Euclidean, may be NULL when train is given)
+ * are the training cores at self-inclusive rank min_samples; when NULL they are computed on the
+ * device. With train NULL (ctx may then be NULL) the predictor is host-only: it serves
+ * cuscan_predictor_predict_candidates only. Errors are also written to err.
+ */
+int cuscan_predictor_create(cuscan_ctx *ctx, const float *train, int64_t n_finite, int32_t d,
+                            int32_t min_samples, const int64_t *tree_parent,
+                            const int64_t *tree_child, const float *tree_lambda,
+                            const float *tree_child_size, int64_t tree_rows,
+                            const int32_t *labels, int64_t raw_n, const uint32_t *finite_index,
+                            const double *prediction_core, cuscan_predictor **out, char *err,
+                            size_t err_len);
+void cuscan_predictor_destroy(cuscan_predictor *p);
+/* 1 when the fitted tree has no clusters (every prediction is noise, 0, -1). */
+int cuscan_predictor_no_cluster_tree(const cuscan_predictor *p);
+int cuscan_predictor_read_cores(const cuscan_predictor *p, double *out);
+/* Predict m finite query rows (host, [m * d]): exact candidate search on the context's device,
+ * then the host candidate math. labels[m], strengths[m] (f64), connecting_points[m] (raw
+ * training rows). */
+int cuscan_predictor_predict(cuscan_ctx *ctx, const cuscan_predictor *p, const float *queries,
+                             int64_t m, int32_t *labels, double *strengths,
+                             int32_t *connecting_points);
+/* The candidate math alone on given rows of width 2 * min_samples: compact ids and Euclidean
+ * distances, ordered as the exact search orders them. */
+int cuscan_predictor_predict_candidates(const cuscan_predictor *p, const int32_t *ids,
+                                        const double *distances, int64_t m, int32_t *labels,
+                                        double *strengths, int32_t *connecting_points, char *err,
+                                        size_t err_len);
+
+/* ---------------------------------------------------------------------------------------
  * Workspace accounting. No reference counterpart: the reference allocates through Burn's
  * memory pool. These let a caller budget device memory around the fit core.
  * ------------------------------------------------------------------------------------- */

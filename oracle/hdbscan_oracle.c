@@ -741,3 +741,243 @@ int orc_finalize_mst(const uint32_t *src, const uint32_t *dst, const float *wsq,
     free(e);
     return ORC_OK;
 }
+
+/* ------------------------------------------------------------------------------------------
+ * approximate_predict (crates/hdbscan-core/src/prediction.rs). The hierarchy follows
+ * PredictionHierarchy::new (prediction.rs:433-700) on a raw-id condensed tree; dense arrays
+ * indexed by raw id stand in for the reference's hash maps. Prediction follows predict_row
+ * (prediction.rs:855-925). Query candidates come from orc_exact_neighbors with self included
+ * (crates/hdbscan/src/prediction.rs:1806-1978), cores from prediction.rs:94-120.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Training prediction cores: self-inclusive exact rows of width s, Euclidean value at rank
+ * s - 1 (0 for s == 1). */
+int orc_prediction_cores(const float *train, int64_t n, int d, int s, double *out) {
+    if (s <= 0 || n <= 0) return ORC_INVALID_INPUT;
+    if (s == 1) {
+        for (int64_t i = 0; i < n; ++i) out[i] = 0.0;
+        return ORC_OK;
+    }
+    int32_t *ids = (int32_t *)malloc(sizeof(int32_t) * (size_t)n * s);
+    float *sq = (float *)malloc(sizeof(float) * (size_t)n * s);
+    if (!ids || !sq) {
+        free(ids);
+        free(sq);
+        return ORC_MEMORY;
+    }
+    int rc = orc_exact_neighbors(train, n, train, n, d, s, 0, 0, 1, ids, sq);
+    for (int64_t i = 0; rc == ORC_OK && i < n; ++i) {
+        const float v = sq[i * s + s - 1];
+        if (!(v >= 0.0f) || v == ORC_INF) rc = ORC_NUMERICAL;
+        else out[i] = sqrt((double)v);
+    }
+    free(ids);
+    free(sq);
+    return rc;
+}
+
+static int finite_pos(const uint32_t *fi, int64_t nf, int64_t raw) {
+    int64_t lo = 0, hi = nf;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        if ((int64_t)fi[mid] < raw) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < nf && (int64_t)fi[lo] == raw) ? (int)lo : -1;
+}
+
+/* Predict m rows from candidate rows of width 2 s (compact ids, Euclidean f64 distances).
+ * Returns ORC_OK, or the error class; *no_cluster is set when the tree has no clusters (the
+ * outputs are then noise, 0, -1). */
+int orc_predict_candidates(const int64_t *parent, const int64_t *child, const float *lambda,
+                           const float *child_size, int64_t rows, const int32_t *labels,
+                           int64_t raw_n, const uint32_t *finite_index, int64_t nf, int s,
+                           const double *cores, const int32_t *cand_ids, const double *cand_dist,
+                           int64_t m, int32_t *out_label, double *out_strength,
+                           int32_t *out_conn, int *no_cluster) {
+    int rc = ORC_OK;
+    int64_t max_id = raw_n;
+    for (int64_t r = 0; r < rows; ++r) {
+        if (parent[r] < raw_n || child[r] < 0) return ORC_INVALID_INPUT;
+        if (parent[r] > max_id) max_id = parent[r];
+        if (child[r] > max_id) max_id = child[r];
+        if (isnan(lambda[r]) || lambda[r] < 0.0f) return ORC_INVALID_INPUT;
+        if (!(child_size[r] >= 1.0f) || child_size[r] == ORC_INF) return ORC_INVALID_INPUT;
+        const int is_point = child[r] < raw_n, is_cluster = child_size[r] > 1.0f;
+        if (is_point == is_cluster) return ORC_INVALID_INPUT;
+        if (is_cluster && child[r] <= parent[r]) return ORC_INVALID_INPUT;
+    }
+    int64_t clusters = 0;
+    for (int64_t r = 0; r < rows; ++r) clusters += child_size[r] > 1.0f;
+    *no_cluster = clusters == 0;
+    if (clusters == 0) {
+        for (int64_t q = 0; q < m; ++q) {
+            out_label[q] = -1;
+            out_strength[q] = 0.0;
+            out_conn[q] = -1;
+        }
+        return ORC_OK;
+    }
+    if (2 * (int64_t)s > nf) return ORC_INVALID_INPUT;
+    const int64_t nn = clusters + 1;
+    int64_t *node_of = (int64_t *)malloc(sizeof(int64_t) * (size_t)(max_id + 1));
+    int64_t *nid = (int64_t *)malloc(sizeof(int64_t) * nn);
+    int64_t *npar = (int64_t *)malloc(sizeof(int64_t) * nn);
+    double *nbirth = (double *)malloc(sizeof(double) * nn);
+    double *nmax = (double *)malloc(sizeof(double) * nn);
+    double *maxl = (double *)malloc(sizeof(double) * nn);
+    int32_t *nlab = (int32_t *)malloc(sizeof(int32_t) * nn);
+    int64_t *anchor_of_label = NULL;  /* smallest parent id per label */
+    int32_t *anchor_label = (int32_t *)malloc(sizeof(int32_t) * nn);
+    int64_t *pnode = (int64_t *)malloc(sizeof(int64_t) * (size_t)nf);
+    double *pdep = (double *)malloc(sizeof(double) * (size_t)nf);
+    int32_t max_label = -1;
+    for (int64_t r = 0; r < raw_n; ++r)
+        if (labels[r] > max_label) max_label = labels[r];
+    anchor_of_label = (int64_t *)malloc(sizeof(int64_t) * (size_t)(max_label + 2));
+    if (!node_of || !nid || !npar || !nbirth || !nmax || !maxl || !nlab || !anchor_label ||
+        !pnode || !pdep || !anchor_of_label) {
+        rc = ORC_MEMORY;
+        goto done;
+    }
+    for (int64_t i = 0; i <= max_id; ++i) node_of[i] = -1;
+    {
+        int64_t root = INT64_MAX;
+        for (int64_t r = 0; r < rows; ++r)
+            if (child_size[r] > 1.0f && parent[r] < root) root = parent[r];
+        node_of[root] = 0;
+        nid[0] = root;
+        npar[0] = -1;
+        nbirth[0] = 0.0;
+        int64_t k = 1;
+        for (int64_t r = 0; r < rows; ++r) {
+            if (!(child_size[r] > 1.0f)) continue;
+            if (node_of[child[r]] >= 0) { rc = ORC_INVALID_INPUT; goto done; }
+            node_of[child[r]] = k;
+            nid[k++] = child[r];
+        }
+        k = 1;
+        for (int64_t r = 0; r < rows; ++r) {
+            if (!(child_size[r] > 1.0f)) continue;
+            if (node_of[parent[r]] < 0) { rc = ORC_INVALID_INPUT; goto done; }
+            npar[k] = node_of[parent[r]];
+            nbirth[k] = (double)lambda[r];
+            ++k;
+        }
+    }
+    for (int64_t i = 0; i < nn; ++i) {
+        maxl[i] = -1.0; /* unseen */
+        anchor_label[i] = -1;
+    }
+    for (int64_t i = 0; i < nf; ++i) pnode[i] = -1;
+    for (int32_t l = 0; l <= max_label; ++l) anchor_of_label[l] = -1;
+    for (int64_t r = 0; r < rows; ++r) {
+        const int64_t node = node_of[parent[r]];
+        if (node < 0) { rc = ORC_INVALID_INPUT; goto done; }
+        const double l = (double)lambda[r];
+        if (maxl[node] < 0.0 || l > maxl[node]) maxl[node] = l;
+        const int pos = child[r] < raw_n ? finite_pos(finite_index, nf, child[r]) : -1;
+        if (pos < 0) continue;
+        if (pnode[pos] >= 0) { rc = ORC_INVALID_INPUT; goto done; }
+        pnode[pos] = node;
+        pdep[pos] = l;
+        const int32_t lab = labels[child[r]];
+        if (lab >= 0 && (anchor_of_label[lab] < 0 || parent[r] < anchor_of_label[lab]))
+            anchor_of_label[lab] = parent[r];
+    }
+    for (int64_t i = 0; i < nf; ++i)
+        if (pnode[i] < 0) { rc = ORC_INVALID_INPUT; goto done; }
+    for (int32_t l = 0; l <= max_label; ++l) {
+        if (anchor_of_label[l] < 0) continue;
+        const int64_t node = node_of[anchor_of_label[l]];
+        if (anchor_label[node] >= 0) { rc = ORC_INVALID_INPUT; goto done; }
+        anchor_label[node] = l;
+    }
+    /* parents precede children in node order? Not in general: resolve by walking up with
+     * memoisation, a node's value being its own anchor's or its parent's. */
+    {
+        int8_t *done_flag = (int8_t *)calloc((size_t)nn, 1);
+        int64_t *path = (int64_t *)malloc(sizeof(int64_t) * nn);
+        if (!done_flag || !path) {
+            free(done_flag);
+            free(path);
+            rc = ORC_MEMORY;
+            goto done;
+        }
+        for (int64_t i = 0; i < nn; ++i) {
+            int64_t len = 0, v = i;
+            while (v >= 0 && !done_flag[v]) {
+                if (len >= nn) { rc = ORC_INVALID_INPUT; break; }  /* a cycle */
+                path[len++] = v;
+                v = npar[v];
+            }
+            if (rc) break;
+            for (int64_t j = len - 1; j >= 0; --j) {
+                const int64_t u = path[j];
+                if (anchor_label[u] >= 0) {
+                    nlab[u] = anchor_label[u];
+                    nmax[u] = maxl[u] < 0.0 ? 0.0 : maxl[u];
+                } else if (npar[u] >= 0) {
+                    nlab[u] = nlab[npar[u]];
+                    nmax[u] = nmax[npar[u]];
+                } else {
+                    nlab[u] = -1;
+                    nmax[u] = 0.0;
+                }
+                done_flag[u] = 1;
+            }
+        }
+        free(done_flag);
+        free(path);
+        if (rc) goto done;
+    }
+    for (int64_t q = 0; q < m && rc == ORC_OK; ++q) {
+        const int32_t *ids = cand_ids + q * 2 * s;
+        const double *dist = cand_dist + q * 2 * s;
+        const double qcore = dist[s];
+        int best = -1;
+        double bmrd = 0.0;
+        for (int c = 0; c < 2 * s; ++c) {
+            if (!(dist[c] >= 0.0) || dist[c] == INFINITY) { rc = ORC_NUMERICAL; break; }
+            if (ids[c] < 0 || ids[c] >= nf) { rc = ORC_NUMERICAL; break; }
+            const double core = cores[ids[c]];
+            double mrd = core > qcore ? core : qcore;
+            if (dist[c] > mrd) mrd = dist[c];
+            if (best < 0 || mrd < bmrd) {
+                best = c;
+                bmrd = mrd;
+            }
+        }
+        if (rc) break;
+        const int32_t conn = ids[best];
+        const double lam = bmrd > 0.0 ? 1.0 / bmrd : 1.7976931348623157e308;
+        int64_t cl = pnode[conn];
+        if (pdep[conn] > lam) {
+            while (nid[cl] > nid[0] && npar[cl] >= 0 && nbirth[cl] >= lam) cl = npar[cl];
+        }
+        if (nlab[cl] < 0) {
+            out_label[q] = -1;
+            out_strength[q] = 0.0;
+        } else if (nmax[cl] > 0.0) {
+            out_label[q] = nlab[cl];
+            out_strength[q] = (nmax[cl] < lam ? nmax[cl] : lam) / nmax[cl];
+        } else {
+            out_label[q] = nlab[cl];
+            out_strength[q] = 1.0;
+        }
+        out_conn[q] = (int32_t)finite_index[conn];
+    }
+done:
+    free(node_of);
+    free(nid);
+    free(npar);
+    free(nbirth);
+    free(nmax);
+    free(maxl);
+    free(nlab);
+    free(anchor_label);
+    free(pnode);
+    free(pdep);
+    free(anchor_of_label);
+    return rc;
+}

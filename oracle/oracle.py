@@ -62,6 +62,11 @@ def lib():
         L.orc_finalize_mst.argtypes = [_U32P, _U32P, _F32P, C.c_int64, _F64P]
         L.orc_pair_distances.argtypes = [_F32P, _F32P, C.c_int64, C.c_int, C.c_int, _F32P]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_prediction_cores.argtypes = [_F32P, C.c_int64, C.c_int, C.c_int, _F64P]
+        L.orc_predict_candidates.argtypes = [_I64P, _I64P, _F32P, _F32P, C.c_int64, _I32P,
+                                             C.c_int64, _U32P, C.c_int64, C.c_int, _F64P, _I32P,
+                                             _F64P, C.c_int64, _I32P, _F64P, _I32P,
+                                             C.POINTER(C.c_int)]
         L.orc_max_threads.restype = C.c_int
         _LIB = L
     return _LIB
@@ -263,3 +268,52 @@ def pair_distances(x, y, *, fused: bool = True) -> np.ndarray:
     out = np.empty(m, np.float32)
     lib().orc_pair_distances(_p(x, _F32P), _p(y, _F32P), m, d, int(fused), _p(out, _F32P))
     return out
+
+
+def prediction_cores(train, min_samples: int) -> np.ndarray:
+    """Training prediction cores (self-inclusive rank s - 1, Euclidean f64)."""
+    train = np.ascontiguousarray(train, np.float32)
+    out = np.empty(train.shape[0], np.float64)
+    _check(lib().orc_prediction_cores(_p(train, _F32P), train.shape[0], train.shape[1],
+                                      int(min_samples), _p(out, _F64P)), "prediction_cores")
+    return out
+
+
+def predict_candidates(tree, labels, finite_index, min_samples: int, cores, ids, distances):
+    """(labels, strengths, connecting points, no_cluster_tree) from candidate rows of width
+    2 * min_samples (compact ids, Euclidean distances). ``tree`` has the condensed-tree fields
+    parent, child, lambda_val, child_size (raw ids)."""
+    parent = np.ascontiguousarray(tree["parent"], np.int64)
+    child = np.ascontiguousarray(tree["child"], np.int64)
+    lam = np.ascontiguousarray(tree["lambda_val"], np.float32)
+    size = np.ascontiguousarray(tree["child_size"], np.float32)
+    labels = np.ascontiguousarray(labels, np.int32)
+    fi = np.ascontiguousarray(finite_index, np.uint32)
+    cores = np.ascontiguousarray(cores, np.float64)
+    ids = np.ascontiguousarray(ids, np.int32)
+    distances = np.ascontiguousarray(distances, np.float64)
+    m = ids.shape[0]
+    out_l = np.empty(m, np.int32)
+    out_s = np.empty(m, np.float64)
+    out_c = np.empty(m, np.int32)
+    nc = C.c_int(0)
+    _check(lib().orc_predict_candidates(
+        _p(parent, _I64P), _p(child, _I64P), _p(lam, _F32P), _p(size, _F32P), parent.shape[0],
+        _p(labels, _I32P), labels.shape[0], _p(fi, _U32P), fi.shape[0], int(min_samples),
+        _p(cores, _F64P), _p(ids, _I32P), _p(distances, _F64P), m, _p(out_l, _I32P),
+        _p(out_s, _F64P), _p(out_c, _I32P), C.byref(nc)), "predict_candidates")
+    return out_l, out_s, out_c, bool(nc.value)
+
+
+def approximate_predict(tree, labels, finite_index, min_samples: int, train, queries,
+                        cores=None):
+    """The whole prediction on the CPU: exact self-inclusive candidates of width 2 s against the
+    finite training rows, then the hierarchy math."""
+    s = int(min_samples)
+    train = np.ascontiguousarray(train, np.float32)
+    queries = np.ascontiguousarray(queries, np.float32)
+    if cores is None:
+        cores = prediction_cores(train, s)
+    ids, sq = exact_neighbors(queries, train, 2 * s, exclude_self=False)
+    return predict_candidates(tree, labels, finite_index, s, cores, ids,
+                              np.sqrt(sq.astype(np.float64)))

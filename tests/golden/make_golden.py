@@ -4,7 +4,10 @@ The reference (lega0208/cuscan) pins its exact HDBSCAN path with 19 fixture case
 ``fast_hdbscan==0.3.2`` (``crates/hdbscan/tests/fixtures/{case}.npz`` + ``{case}.json``,
 listed in ``manifest.json``). This script copies the arrays and parameters of each case, as
 they are, into one compressed ``{case}.npz`` here plus ``manifest.json``, so that tests run
-without the reference checkout. Run it where the reference is mounted:
+without the reference checkout. It also copies ``hdbscan_prediction.json`` (the
+``approximate_predict`` fixture generated by the reference from the original ``hdbscan``
+package: controlled trees, fitted models with candidate rows and expected predictions) as it is.
+Run it where the reference is mounted:
 
     python tests/golden/make_golden.py /root/reference
 """
@@ -40,6 +43,8 @@ def main(reference_root: str) -> None:
             "tie_classification": meta.get("tie_classification"),
             "reason": meta.get("reason"),
         })
+    (HERE / "hdbscan_prediction.json").write_text(
+        (fixtures / "hdbscan_prediction.json").read_text())
     (HERE / "manifest.json").write_text(json.dumps({
         "source": "crates/hdbscan/tests/fixtures (lega0208/cuscan v0.1.3)",
         "generator": manifest["reference"]["package"] + "==" + manifest["reference"]["version"],
