@@ -570,14 +570,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         pre_c.z = col + 2 < P.n ? P.core[col + 2] : 0.0f;
                         pre_c.w = col + 3 < P.n ? P.core[col + 3] : 0.0f;
                     }
-                    pre_c.x *= P.s2;
-                    pre_c.y *= P.s2;
-                    pre_c.z *= P.s2;
-                    pre_c.w *= P.s2;
                     const int64_t ch = t * 8 + half * 4 + (lane & 3);
                     pre_ch = -2;
                     if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
-                    pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i]) * P.s2
+                    pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i])
                                    : CUSCAN_INF;
                 }
             };
@@ -596,11 +592,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     reinterpret_cast<float4 *>(pb)[lane] =
                         make_float4(pre_p.x * sc, pre_p.y * sc, pre_p.z * sc, pre_p.w * sc);
                     reinterpret_cast<float4 *>(mb)[lane] = pre_m;
-                    if (BORUVKA) reinterpret_cast<float4 *>(cb)[lane] = pre_c;
+                    // cores and the component bound come in raw units; the values fetched one
+                    // tile ahead are scaled only here, where they are consumed, so that the
+                    // loads stay in flight behind the previous tile's work
+                    if (BORUVKA)
+                        reinterpret_cast<float4 *>(cb)[lane] =
+                            make_float4(pre_c.x * P.s2, pre_c.y * P.s2, pre_c.z * P.s2,
+                                        pre_c.w * P.s2);
                 }
                 const float mt = pre_mt;
                 const int32_t ch_word = pre_ch;
-                const float comp_bound = pre_cb;
+                const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
                 if (ti_next < P.n_tiles) prefetch(tile_order(P, wa, ti_next));
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }

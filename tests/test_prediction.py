@@ -183,7 +183,13 @@ def test_device_prediction_matches_fixture(cid, case):
     assert_rel(p.cores(), floats(case["prediction_core_distances"]))
     lab, st, conn = p.predict(queries)
     np.testing.assert_array_equal(lab, exp["labels"])
-    np.testing.assert_array_equal(conn, exp["connecting_points_compact"])
+    # the fixture's candidate order among exact ties comes from the original package's search;
+    # the reference exempts the connector identity of those queries (and only that):
+    # python/tests/test_hdbscan_prediction.py:263-270
+    sensitive = {t["query"] for t in case["tie_annotations"] if t["connector_order_sensitive"]}
+    stable = [i for i in range(len(queries)) if i not in sensitive]
+    np.testing.assert_array_equal(conn[stable],
+                                  np.asarray(exp["connecting_points_compact"])[stable])
     assert_rel(st, floats(exp["strengths"]))
     ol, os_, oc, _ = O.approximate_predict(tree, labels, compact, s, train, queries)
     np.testing.assert_array_equal(lab, ol)
