@@ -57,6 +57,10 @@ def parse():
                    help="distinct point sets the request stream cycles through")
     p.add_argument("--serve-slots", type=int, default=8)
     p.add_argument("--serve-precisions", default="bf16_refined,fp16_refined,fp32")
+    p.add_argument("--mixed-predictors", type=int, default=64,
+                   help="resident predictors of the mixed fit/predict stream (0: skip it)")
+    p.add_argument("--mixed-requests", type=int, default=4000)
+    p.add_argument("--mixed-precisions", default="fp16_refined,bf16_refined")
     p.add_argument("--serve-load", type=float, default=0.7,
                    help="Poisson arrival rate as a fraction of the measured saturation rate")
     return p.parse_args()
@@ -321,12 +325,139 @@ def serving_run(args, precision: str) -> dict:
     }
 
 
+def mixed_serving_section(args) -> dict:
+    """Fit requests (the stream above) interleaved with approximate_predict batches (size
+    log-uniform in [1, 4096]) against resident predictors, each fitted on n=100,000, d=64
+    Gaussian mixtures of 40 blobs. Latency per request type; a sample of predictions is
+    compared bit for bit with the same predictor's result computed alone."""
+    import torch
+
+    import cuscan_gb300 as cg
+    from cuscan_gb300 import synthetic
+    from cuscan_gb300.serving import FitServer
+
+    t_setup = time.perf_counter()
+    npred = args.mixed_predictors
+    predictors = []
+    for i in range(npred):
+        x = synthetic.gaussian_mixture(100_000, 64, 40, seed=9000 + i)
+        model = cg.HDBSCAN(min_cluster_size=500, min_samples=5,
+                           precision="fp16_refined").fit(x)
+        predictors.append(model.to_predictor())
+        del x
+    rng = np.random.default_rng(11)
+    pool_n = 256
+    qsizes = np.exp(rng.uniform(np.log(1), np.log(4096), size=pool_n)).astype(np.int64)
+    qpred = rng.integers(0, npred, size=pool_n)
+    qpool = [synthetic.gaussian_mixture(int(qsizes[i]) + 7919, 64, 40,
+                                        seed=9000 + int(qpred[i]))[-int(qsizes[i]):]
+             for i in range(pool_n)]
+    specs = synthetic.fit_request_stream(min(256, args.serve_requests))
+    fpool = [synthetic.request_points(sp) for sp in specs]
+    setup_s = time.perf_counter() - t_setup
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(0.5 * free)
+    out = {"predictors": npred, "predictor_training": "n=100000, d=64, 40 blobs, fp16_refined",
+           "predict_batch": "log-uniform [1, 4096] rows", "setup_s": setup_s}
+
+    def submit(srv, i, prec, kinds):
+        if kinds[i]:
+            j = i % pool_n
+            return srv.submit_predict(predictors[int(qpred[j])], qpool[j])
+        sp = specs[i % len(specs)]
+        return srv.submit(fpool[i % len(fpool)], min_cluster_size=sp["min_cluster_size"],
+                          min_samples=sp["min_samples"], precision=prec)
+
+    def run(srv, count, rate, prec):
+        rs = np.random.default_rng(5)
+        kinds = rs.random(count) < 0.5
+        arrivals = (np.zeros(count) if rate is None
+                    else np.cumsum(rs.exponential(1.0 / rate, size=count)))
+        lag, recs, errors = {}, [], []
+        done = threading.Event()
+
+        def collect():
+            try:
+                got = 0
+                while got < count:
+                    rid = srv.wait_any(5.0)
+                    if rid is None:
+                        continue
+                    info = srv.wait(rid, 0.0)
+                    for _ in range(100000):
+                        if rid in lag:
+                            break
+                        time.sleep(1e-4)
+                    recs.append((info["kind"], lag[rid] + info["latency_ms"], info["n"],
+                                 info["status"]))
+                    srv.release(rid)
+                    got += 1
+            except BaseException as exc:
+                errors.append(exc)
+            finally:
+                done.set()
+
+        th = threading.Thread(target=collect, daemon=True)
+        th.start()
+        t0 = time.perf_counter()
+        for i in range(count):
+            if errors:
+                break
+            target = t0 + arrivals[i]
+            now = time.perf_counter()
+            if target > now:
+                time.sleep(target - now)
+            sub = time.perf_counter()
+            rid = submit(srv, i, prec, kinds)
+            lag[rid] = max(0.0, (sub - target) * 1e3)
+        if not done.wait(timeout=600.0):
+            raise RuntimeError("mixed serving run did not finish within 600 s")
+        span = time.perf_counter() - t0
+        th.join()
+        if errors:
+            raise errors[0]
+        return np.asarray(recs, dtype=np.float64), span
+
+    for prec in args.mixed_precisions.split(","):
+        with FitServer(slots=args.serve_slots, budget_bytes=budget) as srv:
+            kinds = np.arange(2 * args.serve_slots) % 2 == 1
+            for i in range(2 * args.serve_slots):
+                srv.result(submit(srv, i, prec, kinds), timeout=300.0)
+            sat, sat_span = run(srv, min(1000, args.mixed_requests), None, prec)
+            capacity = sat.shape[0] / sat_span
+            rate = args.serve_load * capacity
+            recs, span = run(srv, args.mixed_requests, rate, prec)
+            # a sample of predictions in the mix against the same predictor alone
+            same = True
+            for j in range(16):
+                rid = srv.submit_predict(predictors[int(qpred[j])], qpool[j])
+                r = srv.result(rid, timeout=60.0)
+                lab, st, conn = predictors[int(qpred[j])].approximate_predict(
+                    qpool[j], return_connecting_points=True)
+                same &= (np.array_equal(r["labels"], lab) and np.array_equal(
+                    r["strengths"].view(np.uint64), st.view(np.uint64)) and
+                    np.array_equal(r["connecting_points"], conn))
+        res = {"saturation_req_per_s": capacity, "rate_req_per_s": rate,
+               "requests": int(recs.shape[0]), "req_per_s": recs.shape[0] / span,
+               "failures": int(np.sum(recs[:, 3] != 0)), "predict_mix_equals_alone": bool(same)}
+        for kind, name in ((0, "fit"), (1, "predict")):
+            r = recs[recs[:, 0] == kind]
+            if len(r):
+                res[name] = {"requests": int(len(r)), "p50_ms": float(np.percentile(r[:, 1], 50)),
+                             "p99_ms": float(np.percentile(r[:, 1], 99)),
+                             "mean_rows": float(r[:, 2].mean())}
+        out[prec] = res
+    return out
+
+
 def serving_section(args) -> dict:
     out = {"workload": "gaussian mixtures, n log-uniform [500, 50000], d in {16,32,64,128}, "
                        "2-30 blobs (std U[0.5,2]), min_samples 5, min_cluster_size max(5, n/200)",
            "latency": "arrival -> labels and strengths ready on the host"}
     for prec in args.serve_precisions.split(","):
         out[prec] = serving_run(args, prec)
+    if args.mixed_predictors > 0:
+        out["mixed"] = mixed_serving_section(args)
     return out
 
 

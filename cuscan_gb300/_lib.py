@@ -80,6 +80,10 @@ SIGNATURES = {
     "cuscan_server_wait": (C.c_int, [_VP, C.c_int64, C.c_double, _VP]),
     "cuscan_server_wait_any": (C.c_int, [_VP, C.c_double, _I64P]),
     "cuscan_server_read_fit": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP, _VP]),
+    "cuscan_server_submit_predict": (C.c_int, [_VP, _VP, _VP, C.c_int64, _I64P]),
+    "cuscan_server_read_predict": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP]),
+    "cuscan_predictor_shape": (C.c_int, [_VP, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "cuscan_predict_workspace_bytes": (C.c_int64, [_VP, C.c_int64]),
     "cuscan_server_request_error": (C.c_int, [_VP, C.c_int64, C.c_char_p, C.c_size_t]),
     "cuscan_server_release": (C.c_int, [_VP, C.c_int64]),
     "cuscan_server_get_stats": (C.c_int, [_VP, _VP]),
@@ -122,6 +126,8 @@ class ServerInfo(C.Structure):
         ("request_id", C.c_int64),
         ("status", C.c_int32),
         ("slot", C.c_int32),
+        ("kind", C.c_int32),
+        ("pad", C.c_int32),
         ("n", C.c_int64),
         ("finite_rows", C.c_int64),
         ("d", C.c_int32),
@@ -139,7 +145,8 @@ class ServerInfo(C.Structure):
     ]
 
     def as_dict(self) -> dict:
-        out = {name: getattr(self, name) for name, _ in self._fields_ if name != "stats"}
+        out = {name: getattr(self, name) for name, _ in self._fields_
+               if name not in ("stats", "pad")}
         out["stats"] = self.stats.as_dict()
         return out
 

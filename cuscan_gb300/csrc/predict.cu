@@ -406,6 +406,23 @@ void cuscan_predictor_destroy(cuscan_predictor *p) {
     delete p;
 }
 
+int cuscan_predictor_shape(const cuscan_predictor *p, int64_t *n_finite, int32_t *d,
+                           int32_t *min_samples) {
+    if (!p) return CUSCAN_INVALID_INPUT;
+    if (n_finite) *n_finite = p->n_finite;
+    if (d) *d = p->d;
+    if (min_samples) *min_samples = p->s;
+    return CUSCAN_OK;
+}
+
+int64_t cuscan_predict_workspace_bytes(const cuscan_predictor *p, int64_t m) {
+    if (!p || m <= 0) return 0;
+    const int64_t k = 2 * (int64_t)p->s;
+    // query rows, candidate ids and distances, split-search partial lists
+    const int64_t split = 8 * k * 128 * (4 * (int64_t)kSMs + ceil_div(m, (int64_t)128));
+    return (int64_t)sizeof(float) * m * p->d + 8 * m * k + split + (1 << 20);
+}
+
 int cuscan_predictor_no_cluster_tree(const cuscan_predictor *p) {
     return p && p->node_id.empty() ? 1 : 0;
 }

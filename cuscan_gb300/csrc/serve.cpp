@@ -48,8 +48,12 @@ void set_err(char *err, size_t len, const char *msg) {
     if (err && len) std::snprintf(err, len, "%s", msg);
 }
 
+enum class Kind { Fit = 0, Predict = 1 };
+
 struct Request {
     int64_t id = 0;
+    Kind kind = Kind::Fit;
+    const cuscan_predictor *predictor = nullptr;  // predict requests
     const float *x = nullptr;
     int64_t n = 0;
     int32_t d = 0;
@@ -71,6 +75,8 @@ struct Request {
     std::vector<float> core;
     std::vector<double> sorted_mst;
     cuscan_fit_stats stats{};
+    std::vector<double> strengths;      // predict requests
+    std::vector<int32_t> connectors;
 };
 
 enum class Task { None, Fit, Release, Stop };
@@ -96,6 +102,7 @@ struct Executor {
 
 struct DeviceExecutor : Executor {
     void run(Slot &slot, Request &r) override;
+    void predict(Slot &slot, Request &r);
     void release(Slot &slot) override { cuscan_ctx_release_workspace(slot.ctx); }
     int64_t reserved(Slot &slot) override { return cuscan_ctx_reserved_bytes(slot.ctx); }
 };
@@ -116,7 +123,25 @@ struct SimulatedExecutor : Executor {
     int64_t reserved(Slot &slot) override { return held[index(slot)]; }
 };
 
+// approximate_predict of one query batch against a resident predictor.
+void DeviceExecutor::predict(Slot &slot, Request &r) {
+    const Clock::time_point t0 = Clock::now();
+    r.labels.resize((size_t)r.n);
+    r.strengths.resize((size_t)r.n);
+    r.connectors.resize((size_t)r.n);
+    r.finite_rows = r.n;
+    const int rc = cuscan_predictor_predict(slot.ctx, r.predictor, r.x, r.n, r.labels.data(),
+                                            r.strengths.data(), r.connectors.data());
+    r.fit_ms = ms_between(t0, Clock::now());
+    r.status = rc;
+    if (rc) r.error = cuscan_last_error(slot.ctx);
+}
+
 void DeviceExecutor::run(Slot &slot, Request &r) {
+    if (r.kind == Kind::Predict) {
+        predict(slot, r);
+        return;
+    }
     const Clock::time_point t0 = Clock::now();
     const int64_t n = r.n;
     const int32_t d = r.d;
@@ -306,9 +331,35 @@ struct cuscan_server {
         }
     }
 
+    // Queue a request (or finish it at once when its bound exceeds the budget).
+    int enqueue(std::unique_ptr<Request> r, int64_t *request_id) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (stopping) return CUSCAN_INVALID_INPUT;
+        r->id = next_id++;
+        *request_id = r->id;
+        ++submitted;
+        Request *raw = r.get();
+        requests.emplace(r->id, std::move(r));
+        if (raw->bytes > budget) {
+            raw->status = CUSCAN_MEMORY;
+            raw->error = "the request's workspace bound exceeds the server's memory budget";
+            raw->done = true;
+            raw->t_admit = raw->t_done = raw->t_submit;
+            ++completed;
+            ++failed;
+            finished.push_back(raw->id);
+            cv_done.notify_all();
+            return CUSCAN_OK;
+        }
+        queue.push_back(raw);
+        schedule_locked();
+        return CUSCAN_OK;
+    }
+
     void fill_info(const Request &r, cuscan_server_info *info) const {
         std::memset(info, 0, sizeof(*info));
         info->request_id = r.id;
+        info->kind = (int32_t)r.kind;
         info->status = r.done ? r.status : CUSCAN_PENDING;
         info->slot = r.slot;
         info->n = r.n;
@@ -435,26 +486,45 @@ int cuscan_server_submit_fit(cuscan_server *s, const float *data, int64_t n, int
     r->cfg = *config;
     r->bytes = cuscan_fit_workspace_bytes(n < 2 ? 2 : n, d, min_samples, precision);
     r->t_submit = Clock::now();
+    return s->enqueue(std::move(r), request_id);
+}
+
+int cuscan_server_submit_predict(cuscan_server *s, const cuscan_predictor *predictor,
+                                 const float *queries, int64_t m, int64_t *request_id) {
+    if (!s || !request_id || !predictor) return CUSCAN_INVALID_INPUT;
+    *request_id = 0;
+    if (m <= 0 || (!queries && !s->simulated)) return CUSCAN_INVALID_INPUT;
+    if (m > INT32_MAX) return CUSCAN_OVERFLOW;
+    auto r = std::make_unique<Request>();
+    r->kind = Kind::Predict;
+    r->predictor = predictor;
+    r->x = queries;
+    r->n = m;
+    int64_t nf = 0;
+    int32_t d = 0, ms = 0;
+    cuscan_predictor_shape(predictor, &nf, &d, &ms);
+    r->d = d;
+    r->min_samples = ms;
+    r->bytes = cuscan_predict_workspace_bytes(predictor, m);
+    r->t_submit = Clock::now();
+    return s->enqueue(std::move(r), request_id);
+}
+
+int cuscan_server_read_predict(cuscan_server *s, int64_t request_id, int32_t *labels,
+                               double *strengths, int32_t *connecting_points) {
+    if (!s) return CUSCAN_INVALID_INPUT;
     std::lock_guard<std::mutex> lk(s->mu);
-    if (s->stopping) return CUSCAN_INVALID_INPUT;
-    r->id = s->next_id++;
-    *request_id = r->id;
-    ++s->submitted;
-    Request *raw = r.get();
-    s->requests.emplace(r->id, std::move(r));
-    if (raw->bytes > s->budget) {
-        raw->status = CUSCAN_MEMORY;
-        raw->error = "the request's workspace bound exceeds the server's memory budget";
-        raw->done = true;
-        raw->t_admit = raw->t_done = raw->t_submit;
-        ++s->completed;
-        ++s->failed;
-        s->finished.push_back(raw->id);
-        s->cv_done.notify_all();
-        return CUSCAN_OK;
-    }
-    s->queue.push_back(raw);
-    s->schedule_locked();
+    auto it = s->requests.find(request_id);
+    if (it == s->requests.end()) return CUSCAN_INVALID_INPUT;
+    const Request &r = *it->second;
+    if (r.kind != Kind::Predict) return CUSCAN_INVALID_INPUT;
+    if (!r.done) return CUSCAN_PENDING;
+    if (r.status) return r.status;
+    if (s->simulated) return CUSCAN_INVALID_INPUT;  // the test double computes no result
+    if (labels) std::memcpy(labels, r.labels.data(), r.labels.size() * sizeof(int32_t));
+    if (strengths) std::memcpy(strengths, r.strengths.data(), r.strengths.size() * sizeof(double));
+    if (connecting_points)
+        std::memcpy(connecting_points, r.connectors.data(), r.connectors.size() * sizeof(int32_t));
     return CUSCAN_OK;
 }
 
@@ -492,6 +562,7 @@ int cuscan_server_read_fit(cuscan_server *s, int64_t request_id, int32_t *labels
     auto it = s->requests.find(request_id);
     if (it == s->requests.end()) return CUSCAN_INVALID_INPUT;
     const Request &r = *it->second;
+    if (r.kind != Kind::Fit) return CUSCAN_INVALID_INPUT;
     if (!r.done) return CUSCAN_PENDING;
     if (r.status) return r.status;
     if (s->simulated) return CUSCAN_INVALID_INPUT;  // the test double computes no result

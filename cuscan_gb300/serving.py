@@ -1,10 +1,12 @@
-"""Continuous-batching fit server on one GPU (the ``cuscan_server_*`` C ABI).
+"""Continuous-batching request server on one GPU (the ``cuscan_server_*`` C ABI).
 
-Requests are HDBSCAN fits of independent point sets. They queue in arrival order and are
-admitted onto execution slots (each with its own CUDA stream, workspace and host thread) as
-slots and device memory free up, so that fits of different sizes overlap on the device. A
-request's result is the same as that of ``HDBSCAN(...).fit`` on the same rows (labels,
-membership strengths, core distances, sorted MST), which the tests check bit for bit.
+Requests are HDBSCAN fits of independent point sets and ``approximate_predict`` batches against
+resident predictors. They queue in arrival order and are admitted onto execution slots (each
+with its own CUDA stream, workspace and host thread) as slots and device memory free up, so
+that requests of different sizes overlap on the device. A fit's result is the same as that of
+``HDBSCAN(...).fit`` on the same rows (labels, membership strengths, core distances, sorted
+MST), a prediction's the same as the predictor's own ``approximate_predict``; the tests check
+both bit for bit.
 
 The reference has no serving layer; a request runs the estimator flow of
 crates/hdbscan/src/estimator.rs:1034-1392.
@@ -79,6 +81,24 @@ class FitServer:
             self._inputs[int(rid.value)] = arr
         return int(rid.value)
 
+    def submit_predict(self, predictor, x) -> int:
+        """Queue an approximate_predict of finite query rows against a resident predictor
+        (``cuscan_gb300.prediction.Predictor`` or ``HDBSCANPredictor`` on this device)."""
+        pred = getattr(predictor, "_predictor", predictor)
+        arr = np.ascontiguousarray(x, dtype=np.float32)
+        if arr.ndim != 2 or arr.shape[0] == 0 or arr.shape[1] != pred.n_features_in_:
+            raise ValueError("query rows must be a non-empty 2-D array with the model's features")
+        if not np.all(np.isfinite(arr)):
+            raise ValueError("X must contain only finite values")
+        rid = C.c_int64(0)
+        with self._guard:
+            code = self._lib.cuscan_server_submit_predict(self.handle, pred.handle,
+                                                          arr.ctypes.data, arr.shape[0],
+                                                          C.byref(rid))
+            _lib.raise_for(code, "predict request rejected")
+            self._inputs[int(rid.value)] = (arr, pred)
+        return int(rid.value)
+
     def wait(self, request_id: int, timeout: float | None = None) -> dict | None:
         """Information on a request once it has finished (None on timeout)."""
         info = _lib.ServerInfo()
@@ -102,9 +122,10 @@ class FitServer:
         return int(rid.value)
 
     def result(self, request_id: int, timeout: float | None = None, release: bool = True) -> dict:
-        """Wait for a request and return its fit: labels, probabilities, core_distances,
-        minimum_spanning_tree (sorted, Euclidean) and the request information. Raises the
-        request's own error if it failed."""
+        """Wait for a request and return its result with the request information: for a fit,
+        labels, probabilities, core_distances and minimum_spanning_tree (sorted, Euclidean);
+        for a prediction, labels, strengths and connecting_points. Raises the request's own
+        error if it failed."""
         info = self.wait(request_id, timeout)
         if info is None:
             raise TimeoutError(f"request {request_id} has not finished")
@@ -115,6 +136,16 @@ class FitServer:
                 self._lib.cuscan_server_request_error(self.handle, rid, buf, 512)
                 _lib.raise_for(info["status"], buf.value.decode("utf-8", "replace"))
             n, nf = int(info["n"]), int(info["finite_rows"])
+            if info["kind"] == 1:
+                labels = np.empty(n, np.int32)
+                strengths = np.empty(n, np.float64)
+                conn = np.empty(n, np.int32)
+                code = self._lib.cuscan_server_read_predict(self.handle, rid, labels.ctypes.data,
+                                                            strengths.ctypes.data,
+                                                            conn.ctypes.data)
+                _lib.raise_for(code, "the request's result cannot be read")
+                return {"labels": labels.astype(np.intp), "strengths": strengths,
+                        "connecting_points": conn.astype(np.intp), "info": info}
             labels = np.empty(n, np.int32)
             prob = np.empty(n, np.float32)
             core = np.empty(nf, np.float32)

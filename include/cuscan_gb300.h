@@ -263,6 +263,10 @@ int cuscan_predictor_create(cuscan_ctx *ctx, const float *train, int64_t n_finit
                             const double *prediction_core, cuscan_predictor **out, char *err,
                             size_t err_len);
 void cuscan_predictor_destroy(cuscan_predictor *p);
+int cuscan_predictor_shape(const cuscan_predictor *p, int64_t *n_finite, int32_t *d,
+                           int32_t *min_samples);
+/* Upper bound on the context workspace one cuscan_predictor_predict of m rows allocates. */
+int64_t cuscan_predict_workspace_bytes(const cuscan_predictor *p, int64_t m);
 /* 1 when the fitted tree has no clusters (every prediction is noise, 0, -1). */
 int cuscan_predictor_no_cluster_tree(const cuscan_predictor *p);
 int cuscan_predictor_read_cores(const cuscan_predictor *p, double *out);
@@ -292,10 +296,11 @@ int64_t cuscan_ctx_reserved_bytes(const cuscan_ctx *ctx);
 int cuscan_ctx_release_workspace(cuscan_ctx *ctx);
 
 /* ---------------------------------------------------------------------------------------
- * Fit-request server: continuous batching of HDBSCAN fits on one GPU. No reference
- * counterpart (the reference fits one point set per call); each request runs the estimator
- * flow of crates/hdbscan/src/estimator.rs:1034-1392: finite split, cuscan_fit_core, then
- * cuscan_clusters_from_spanning_tree.
+ * Request server: continuous batching of HDBSCAN fits and approximate_predict batches on one
+ * GPU. No reference counterpart (the reference serves one call at a time). A fit request runs
+ * the estimator flow of crates/hdbscan/src/estimator.rs:1034-1392: finite split,
+ * cuscan_fit_core, then cuscan_clusters_from_spanning_tree; a predict request runs
+ * cuscan_predictor_predict against a resident predictor.
  *
  * Requests queue in arrival order and are admitted onto `slots` execution slots, each with its
  * own CUDA stream, workspace and host thread, as slots and device memory free up: the sum over
@@ -314,6 +319,8 @@ typedef struct cuscan_server_info {
     int64_t request_id;
     int32_t status;          /* outcome once finished; CUSCAN_PENDING while queued or running */
     int32_t slot;            /* slot that ran it, -1 before admission */
+    int32_t kind;            /* 0 fit, 1 approximate_predict */
+    int32_t pad;
     int64_t n;
     int64_t finite_rows;
     int32_t d;
@@ -352,6 +359,14 @@ void cuscan_server_destroy(cuscan_server *server);
 int cuscan_server_submit_fit(cuscan_server *server, const float *data, int64_t n, int32_t d,
                              int32_t min_samples, int32_t precision,
                              const cuscan_extract_config *config, int64_t *request_id);
+/* Queue an approximate_predict of m finite query rows (host, [m * d]) against a resident
+ * predictor created on the server's device. The predictor and the queries stay valid and
+ * unchanged until the request has finished. */
+int cuscan_server_submit_predict(cuscan_server *server, const cuscan_predictor *predictor,
+                                 const float *queries, int64_t m, int64_t *request_id);
+/* labels[m], strengths[m], connecting_points[m] of a finished predict request. */
+int cuscan_server_read_predict(cuscan_server *server, int64_t request_id, int32_t *labels,
+                               double *strengths, int32_t *connecting_points);
 /* Wait up to timeout_ms (< 0: no limit) for one request; CUSCAN_OK once it has finished
  * (info->status is its outcome), CUSCAN_PENDING if it has not. */
 int cuscan_server_wait(cuscan_server *server, int64_t request_id, double timeout_ms,

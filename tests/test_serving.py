@@ -109,6 +109,37 @@ def test_invalid_server_and_request_arguments():
             assert srv.wait(rid, 5.0)["status"] == _lib.OK
 
 
+def host_predictor():
+    from cuscan_gb300.prediction import Predictor
+    labels = np.array([0, 0, 0, 1, 1, 1], np.int32)
+    rows = [(6, 7, 1.0, 3.0), (6, 8, 1.0, 3.0)] + [(7, i, 2.0, 1.0) for i in range(3)] + \
+           [(8, i, 2.0, 1.0) for i in range(3, 6)]
+    t = np.array(rows, dtype=[("parent", np.int64), ("child", np.int64),
+                              ("lambda_val", np.float64), ("child_size", np.float64)])
+    return Predictor(condensed_tree=t, labels=labels, finite_index=np.arange(6, dtype=np.uint32),
+                     min_samples=2, n_features=3, prediction_core=np.zeros(6))
+
+
+def test_predict_requests_share_the_queue_with_fits():
+    pred = host_predictor()
+    with FitServer(slots=2, budget_bytes=1 << 32, simulated_us_per_kpoint=100.0) as srv:
+        ids = []
+        for i in range(20):
+            if i % 2:
+                ids.append(srv.submit_predict(pred, np.zeros((1 + 50 * i, 3), np.float32)))
+            else:
+                ids.append(srv.submit(np.zeros((2000, 3), np.float32), min_cluster_size=5))
+        infos = drain(srv, ids)
+        assert [infos[r]["kind"] for r in ids] == [i % 2 for i in range(20)]
+        assert all(infos[r]["status"] == _lib.OK for r in ids)
+        with pytest.raises(ValueError):  # the test double computes no result
+            srv.result(ids[1])
+        with pytest.raises(ValueError):
+            srv.submit_predict(pred, np.zeros((4, 2), np.float32))   # wrong feature count
+        with pytest.raises(ValueError):
+            srv.submit_predict(pred, np.full((4, 3), np.nan, np.float32))
+
+
 # ---------------------------------------------------------------- GPU ----------------------
 
 def request_mix():
@@ -174,3 +205,35 @@ def test_workspace_bound_covers_a_fit(n, d, ms, prec):
         assert ctx.reserved_bytes() == 0
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+def test_predictions_in_the_mix_equal_predictions_alone():
+    import cuscan_gb300 as cg
+    models, queries = [], []
+    for i, (n, d) in enumerate([(6000, 16), (9000, 64)]):
+        x = synthetic.gaussian_mixture(n, d, 12, seed=300 + i)
+        models.append(cg.HDBSCAN(min_cluster_size=30, min_samples=5,
+                                 precision="fp16_refined").fit(x))
+        queries.append([synthetic.gaussian_mixture(m, d, 12, seed=300 + i) + np.float32(0.05)
+                        for m in (1, 17, 400, 3000)])
+    alone = [[m.approximate_predict(q, return_connecting_points=True) for q in qs]
+             for m, qs in zip(models, queries)]
+    preds = [m.to_predictor() for m in models]
+    mix = request_mix()
+    with FitServer(slots=4, budget_bytes=8 << 30) as srv:
+        ids = []
+        for j in range(4):
+            for i in range(2):
+                ids.append(("p", i, j, srv.submit_predict(preds[i], queries[i][j])))
+            x, mcs, prec = mix[j]
+            ids.append(("f", j, None, srv.submit(x, min_cluster_size=mcs, min_samples=5,
+                                                 precision=prec)))
+        results = [(kind, i, j, srv.result(r, timeout=120.0)) for kind, i, j, r in ids]
+    for kind, i, j, r in results:
+        if kind != "p":
+            continue
+        lab, st, conn = alone[i][j]
+        np.testing.assert_array_equal(r["labels"], lab)
+        np.testing.assert_array_equal(r["strengths"].view(np.uint64), st.view(np.uint64))
+        np.testing.assert_array_equal(r["connecting_points"], conn)
