@@ -38,6 +38,9 @@ constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of 
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded mbarrier waits: 2 s of wall time
 constexpr uint32_t WAIT_POLLS = 1u << 22;      // poll bound of the abort-path drains
 constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
+// per epilogue warp: [2][HALF] scaled norms, [2][HALF] cores, [2][HALF] m, then [2][4] (min
+// scaled norm, min core) of each 32-column chunk
+constexpr int PB_STRIDE = 6 * HALF + 16;
 constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row half
 
 struct Params {
@@ -295,6 +298,24 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
 // per-row thresholds tighten at once), then every other tile in one global order shared by all
 // CTAs, so that the blocks running at the same time stream the same tiles and share them in L2.
 constexpr int64_t WARM = 4;
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Largest of 32 values with three-input maxima.
+__device__ __forceinline__ float max32(const float (&v)[32]) {
+    float t[12];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) t[i] = fmax3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    t[10] = v[30];
+    t[11] = v[31];
+    const float u0 = fmax3(t[0], t[1], t[2]), u1 = fmax3(t[3], t[4], t[5]);
+    const float u2 = fmax3(t[6], t[7], t[8]), u3 = fmax3(t[9], t[10], t[11]);
+    return fmaxf(fmax3(u0, u1, u2), u3);
+}
+
 __device__ __forceinline__ int64_t window_start(const Params &P, int64_t qb) {
     const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
     const int64_t first = P.qpos ? (int64_t)P.qpos[qb * BM] : qb * BM;
@@ -356,8 +377,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     const uint32_t b_bytes = (uint32_t)P.kblocks * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
-    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][6][HALF]
-    float *vstage = pbuf + EPI_WARPS * 6 * HALF;                     // [EPI_WARPS][32][VSTRIDE]
+    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][PB_STRIDE]
+    float *vstage = pbuf + EPI_WARPS * PB_STRIDE;                    // [EPI_WARPS][32][VSTRIDE]
     uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
     uint64_t *full = bars;
     uint64_t *empty = bars + P.stages;
@@ -507,7 +528,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         const int quad = warp & 3;            // TMEM lane quadrant of this warp
         const int half = ew >> 2;             // column half of each tile
         const int row_local = quad * 32 + lane;
-        float *my_pb = pbuf + ew * 6 * HALF;  // [2][HALF] scaled norms, [2][HALF] cores, [2][HALF] m
+        float *my_pb = pbuf + ew * PB_STRIDE;
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
         uint32_t tcount = 0;
         for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
@@ -587,18 +608,33 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 float *pb = my_pb + b * HALF;
                 float *cb = my_pb + (2 + b) * HALF;
                 float *mb = my_pb + (4 + b) * HALF;
+                const float2 *chunk_min = reinterpret_cast<const float2 *>(my_pb + 6 * HALF + b * 8);
                 {
                     const float sc = P.one_minus_cb;
-                    reinterpret_cast<float4 *>(pb)[lane] =
+                    const float4 pv =
                         make_float4(pre_p.x * sc, pre_p.y * sc, pre_p.z * sc, pre_p.w * sc);
+                    reinterpret_cast<float4 *>(pb)[lane] = pv;
                     reinterpret_cast<float4 *>(mb)[lane] = pre_m;
+                    float pmin = fminf(fminf(pv.x, pv.y), fminf(pv.z, pv.w));
+                    float cmin = 0.0f;
                     // cores and the component bound come in raw units; the values fetched one
                     // tile ahead are scaled only here, where they are consumed, so that the
                     // loads stay in flight behind the previous tile's work
-                    if (BORUVKA)
-                        reinterpret_cast<float4 *>(cb)[lane] =
-                            make_float4(pre_c.x * P.s2, pre_c.y * P.s2, pre_c.z * P.s2,
-                                        pre_c.w * P.s2);
+                    if (BORUVKA) {
+                        const float4 cv = make_float4(pre_c.x * P.s2, pre_c.y * P.s2,
+                                                      pre_c.z * P.s2, pre_c.w * P.s2);
+                        reinterpret_cast<float4 *>(cb)[lane] = cv;
+                        cmin = fminf(fminf(cv.x, cv.y), fminf(cv.z, cv.w));
+                    }
+                    // minima over each 32-column chunk (8 lanes of 4 columns)
+#pragma unroll
+                    for (int o = 1; o < 8; o <<= 1) {
+                        pmin = fminf(pmin, __shfl_xor_sync(0xffffffffu, pmin, o));
+                        if (BORUVKA) cmin = fminf(cmin, __shfl_xor_sync(0xffffffffu, cmin, o));
+                    }
+                    if ((lane & 7) == 0)
+                        reinterpret_cast<float2 *>(my_pb + 6 * HALF + b * 8)[lane >> 3] =
+                            make_float2(pmin, cmin);
                 }
                 const float mt = pre_mt;
                 const int32_t ch_word = pre_ch;
@@ -655,21 +691,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
                     const float dlt = thr2 - T;
                     const float thr_fast = thr2 + 0x1p-20f * (fabsf(thr2) + fabsf(T));
-                    float mn = CUSCAN_INF;
-                    if (active && (!BORUVKA || core_i <= T)) {
-                        const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
-                        const float4 *cc = reinterpret_cast<const float4 *>(cb + c * 32);
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const float4 pq = pc[q];
-                            float f0 = fmaf(-2.0f, v[4 * q + 0], pq.x);
-                            float f1 = fmaf(-2.0f, v[4 * q + 1], pq.y);
-                            float f2 = fmaf(-2.0f, v[4 * q + 2], pq.z);
-                            float f3 = fmaf(-2.0f, v[4 * q + 3], pq.w);
-                            mn = fminf(mn, fminf(fminf(f0, f1), fminf(f2, f3)));
-                        }
-                    }
-                    const bool any_hit = mn < thr_fast;
+                    // Coarse test of the whole chunk first: with the chunk's smallest scaled
+                    // norm and core, fmaf(-2, max v, min pb) is below (or equal to) every
+                    // element's fmaf(-2, v_j, pb_j) and core_j + dlt bounds the core term,
+                    // because rounding is monotonic; only chunks that pass it are tested
+                    // element by element.
+                    const float2 cmin = chunk_min[c];
+                    float flb = fmaf(-2.0f, max32(v), cmin.x);
+                    if (BORUVKA) flb = fmaxf(flb, cmin.y + dlt);
+                    const bool any_hit = active && (!BORUVKA || core_i <= T) && flb < thr_fast;
                     if (__any_sync(0xffffffffu, any_hit)) {
                         unsigned hits = 0;
                         if (any_hit) {
@@ -1061,7 +1091,7 @@ static bool refined_layout(int64_t n, int d, Layout &L) {
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
     const size_t a = (size_t)L.kblocks * KBLOCK_A, b = (size_t)L.kblocks * KBLOCK_B;
-    const size_t fixed = a + (size_t)EPI_WARPS * 6 * HALF * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+    const size_t fixed = a + (size_t)EPI_WARPS * PB_STRIDE * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
                          256 + 1024;
     int st = (int)((227 * 1024 - fixed) / b);
     if (st > 4) st = 4;
