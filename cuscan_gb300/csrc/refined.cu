@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         const int row_local = quad * 32 + lane;
         float *my_pb = pbuf + ew * PB_STRIDE;
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
+        const bool debug = P.debug_tile != nullptr && blockIdx.x == 0;
         uint32_t tcount = 0;
         for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
             const int64_t row = qb * BM + row_local;  // query row
@@ -645,62 +646,92 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 const uint32_t taddr =
                     tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN + half * HALF;
-                // TMEM loads are software pipelined: chunk c+1 is in flight while chunk c is
-                // screened (rA/rB alternate; the loop is unrolled so both stay in registers)
-                // (threshold modes only: the kNN list leaves no room for the second buffer)
+                // Phase 1: the largest dot product of each 32-column chunk (TMEM loads are
+                // software pipelined in the threshold modes: the next chunk is in flight while
+                // one is reduced; the kNN list leaves no room for the second buffer).
+                // Phase 2: one coarse test per chunk against this tile's thresholds and one warp
+                // vote per tile; the chunks that pass are read again from TMEM (the buffer is
+                // released only after this tile) and tested element by element.
                 constexpr bool PIPE = APPEND;
-                uint32_t rA[32], rB[PIPE ? 32 : 1];
-                tmem_ld32_issue(taddr, rA);
-                tmem_ld_wait(rA);
+                float vmax[HALF / 32];
+                {
+                    uint32_t rA[32], rB[PIPE ? 32 : 1];
+                    tmem_ld32_issue(taddr, rA);
+                    tmem_ld_wait(rA);
 #pragma unroll
-                for (int c = 0; c < HALF / 32; ++c) {
-                    uint32_t(&rc_)[32] = rA;
-                    if constexpr (PIPE) {
-                        if (c > 0) {
-                            // the chunk loaded into rB during the previous step becomes current
+                    for (int c = 0; c < HALF / 32; ++c) {
+                        if constexpr (PIPE) {
+                            if (c > 0) {
 #pragma unroll
-                            for (int e = 0; e < 32; ++e) rA[e] = rB[e];
+                                for (int e = 0; e < 32; ++e) rA[e] = rB[e];
+                            }
+                            if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
+                        } else if (c > 0) {
+                            tmem_ld32_issue(taddr + c * 32, rA);
+                            tmem_ld_wait(rA);
                         }
-                        if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
-                    } else if (c > 0) {
-                        tmem_ld32_issue(taddr + c * 32, rA);
-                        tmem_ld_wait(rA);
+                        float v[32];
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(rA[e]);
+                        if (debug && tcount == 0) {
+#pragma unroll
+                            for (int e = 0; e < 32; ++e)
+                                P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
+                        }
+                        vmax[c] = max32(v);
+                        if constexpr (PIPE) {
+                            if (c + 1 < HALF / 32) tmem_ld_wait(rB);
+                        }
                     }
+                }
+                // Thresholds moved to the scale of F = (1 - C_B) p_j - 2 dot with the tile's
+                // largest norm, then widened by a few ulps so that no pair whose exact-path
+                // bound would pass is filtered out. For Borůvka the core condition
+                // core_j < T rides along as max(F, core_j + (thr2 - T)). The element path
+                // recomputes them after it lowers U or the list bound; a stale (larger)
+                // threshold only admits more pairs to the exact test.
+                float T = 0.0f, dlt = 0.0f, thr_fast = 0.0f;
+                auto thresholds = [&]() {
+                    T = BORUVKA ? fminf(U, comp_bound) : THRESH ? tau : L[LM - 1];
+                    const float base = T - ps_i + cm_i * mt;
+                    const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
+                    dlt = thr2 - T;
+                    thr_fast = thr2 + 0x1p-20f * (fabsf(thr2) + fabsf(T));
+                };
+                thresholds();
+                // Coarse test of each chunk: with the chunk's smallest scaled norm and core,
+                // fmaf(-2, max v, min pb) is below (or equal to) every element's
+                // fmaf(-2, v_j, pb_j) and min core + dlt bounds the core term, because rounding
+                // is monotonic.
+                unsigned hitbits = 0;
+                {
+                    const bool row_on = valid && tau_ok && (!BORUVKA || core_i <= T);
+#pragma unroll
+                    for (int c = 0; c < HALF / 32; ++c) {
+                        bool on = row_on;
+                        if (BORUVKA) {
+                            const int32_t clo = __shfl_sync(0xffffffffu, ch_word, c);
+                            const int32_t chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
+                            if (clo == -2 || (clo == lab_i && chi == lab_i)) on = false;
+                        }
+                        const float2 cmin = chunk_min[c];
+                        float flb = fmaf(-2.0f, vmax[c], cmin.x);
+                        if (BORUVKA) flb = fmaxf(flb, cmin.y + dlt);
+                        if (on && flb < thr_fast) hitbits |= 1u << c;
+                    }
+                }
+                const unsigned warp_bits = __reduce_or_sync(0xffffffffu, hitbits);
+                for (int c = 0; warp_bits != 0 && c < HALF / 32; ++c) {
+                    if (!((warp_bits >> c) & 1u)) continue;
+                    uint32_t rc_[32];
+                    tmem_ld32_issue(taddr + c * 32, rc_);
+                    tmem_ld_wait(rc_);
                     float v[32];
 #pragma unroll
                     for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(rc_[e]);
-                    if (P.debug_tile && blockIdx.x == 0 && tcount == 0) {
-#pragma unroll
-                        for (int e = 0; e < 32; ++e)
-                            P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
-                    }
-                    bool active = valid && tau_ok;
-                    int32_t clo = 0, chi = 0;
-                    if (BORUVKA) {
-                        clo = __shfl_sync(0xffffffffu, ch_word, c);
-                        chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
-                        if (clo == -2 || (clo == lab_i && chi == lab_i)) active = false;
-                    }
-                    // Fast test on the running minimum of the chunk. thr2 is the list threshold
-                    // moved to the scale of F = (1 - C_B) p_j - 2 dot with the tile's largest
-                    // norm, then widened by a few ulps so that no pair whose exact-path bound
-                    // would enter the list is passed over. For Borůvka the core condition
-                    // core_j < T rides along as max(F, core_j + (thr2 - T)).
-                    const float T = BORUVKA ? fminf(U, comp_bound) : THRESH ? tau : L[LM - 1];
-                    const float base = T - ps_i + cm_i * mt;
-                    const float thr2 = base + 0x1p-21f * (fabsf(T) + ps_i + cm_i * mt);
-                    const float dlt = thr2 - T;
-                    const float thr_fast = thr2 + 0x1p-20f * (fabsf(thr2) + fabsf(T));
-                    // Coarse test of the whole chunk first: with the chunk's smallest scaled
-                    // norm and core, fmaf(-2, max v, min pb) is below (or equal to) every
-                    // element's fmaf(-2, v_j, pb_j) and core_j + dlt bounds the core term,
-                    // because rounding is monotonic; only chunks that pass it are tested
-                    // element by element.
-                    const float2 cmin = chunk_min[c];
-                    float flb = fmaf(-2.0f, max32(v), cmin.x);
-                    if (BORUVKA) flb = fmaxf(flb, cmin.y + dlt);
-                    const bool any_hit = active && (!BORUVKA || core_i <= T) && flb < thr_fast;
-                    if (__any_sync(0xffffffffu, any_hit)) {
+                    const bool any_hit = (hitbits >> c) & 1u;
+                    {
+
                         unsigned hits = 0;
                         if (any_hit) {
                             const float4 *pc = reinterpret_cast<const float4 *>(pb + c * 32);
@@ -729,6 +760,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             for (int q = 0; q < 8; ++q)
                                 reinterpret_cast<float4 *>(my_v)[q] =
                                     make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                        }
+                        int32_t clo = 0, chi = 0;
+                        if (BORUVKA) {
+                            clo = __shfl_sync(0xffffffffu, ch_word, c);
+                            chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
                         }
                         const bool uniform_other = BORUVKA && clo == chi && clo != lab_i;
                         while (hits) {
@@ -768,9 +804,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             }
                         }
                         __syncwarp();
-                    }
-                    if constexpr (PIPE) {
-                        if (c + 1 < HALF / 32) tmem_ld_wait(rB);
+                        thresholds();
                     }
                 }
                 fence_before();
