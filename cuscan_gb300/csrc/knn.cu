@@ -289,7 +289,7 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
     if (qblocks < target) splits = ceil_div(target, qblocks);
     const int64_t max_splits = ceil_div(nr, (int64_t)RT * 8);
     if (splits > max_splits) splits = max_splits;
-    if (splits > 64) splits = 64;
+    if (splits > 1024) splits = 1024;
     if (splits < 1) splits = 1;
     int64_t chunk = ceil_div(ceil_div(nr, splits), RT) * RT;
     splits = ceil_div(nr, chunk);

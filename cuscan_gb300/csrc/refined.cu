@@ -853,6 +853,39 @@ __device__ __forceinline__ float exact_d2(const float *__restrict__ a, const flo
     return acc;
 }
 
+// Exact squared distance (the reference's order) from the warp's query row q_s (shared) to the
+// candidate row j held by this lane (j < 0: none, returns +inf). The warp first copies the 32
+// candidate rows into its shared staging area row by row, each row read with consecutive
+// addresses, then every lane sums its own row sequentially; the row stride d + 1 keeps the
+// lanes on distinct banks.
+__device__ __forceinline__ float staged_d2(const float *__restrict__ x, int d,
+                                           const float *q_s, int32_t j, float *rows_s,
+                                           int lane) {
+    for (int r = 0; r < 32; ++r) {
+        const int32_t jr = __shfl_sync(0xffffffffu, j, r);
+        if (jr < 0) continue;
+        const float *src = x + (int64_t)jr * d;
+        float *dst = rows_s + r * (d + 1);
+        for (int f = lane; f < d; f += 32) dst[f] = src[f];
+    }
+    __syncwarp();
+    float acc = CUSCAN_INF;
+    if (j >= 0) {
+        const float *row = rows_s + lane * (d + 1);
+        acc = 0.0f;
+        for (int f = 0; f < d; ++f) {
+            const float t = q_s[f] - row[f];
+            acc = __fmaf_rn(t, t, acc);
+        }
+    }
+    __syncwarp();
+    return acc;
+}
+
+// Shared floats one warp of a re-rank kernel stages: 32 candidate rows and the query row.
+__host__ __device__ constexpr int64_t rerank_warp_floats(int d) { return 32 * (d + 1) + d; }
+constexpr int RERANK_WARPS = 4;
+
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -883,23 +916,23 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__
                                   float *__restrict__ dist, int32_t *__restrict__ fallback,
                                   float *__restrict__ fallback_thr,
                                   int *__restrict__ fallback_count) {
+    extern __shared__ float rerank_smem[];
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
+    float *q_s = rerank_smem + (threadIdx.x >> 5) * rerank_warp_floats(d);
+    float *rows_s = q_s + d;
+    for (int f = lane; f < d; f += 32) q_s[f] = x[row * d + f];
+    __syncwarp();
     constexpr int W = 2 * M;  // two lists of M per row (one per column half)
     constexpr int PER = W / 32;
     unsigned long long key[PER];
-    const float *xr = x + row * d;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const int s = q * 32 + lane;
         const int32_t j = cand_ids[row * W + s];
-        if (j < 0) {
-            key[q] = ~0ull;
-        } else {
-            const float dd = exact_d2(xr, x + (int64_t)j * d, d);
-            key[q] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
-        }
+        const float dd = staged_d2(x, d, q_s, j, rows_s, lane);
+        key[q] = j < 0 ? ~0ull : ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
     }
     const int64_t orow = perm[row];
     float dk = CUSCAN_INF;
@@ -958,18 +991,21 @@ __global__ void rerank_knn_threshold_kernel(const float *__restrict__ x,
         if (lane == 0) fallback[atomicAdd(fallback_count, 1)] = (int32_t)orow;
         return;
     }
-    const float *xr = x + pos * d;
+    extern __shared__ float rerank_smem[];
+    float *q_s = rerank_smem + (threadIdx.x >> 5) * rerank_warp_floats(d);
+    float *rows_s = q_s + d;
+    for (int f = lane; f < d; f += 32) q_s[f] = x[pos * d + f];
+    __syncwarp();
     unsigned long long key[PER];
 #pragma unroll
     for (int t = 0; t < PER; ++t) {
         const int s = lane + 32 * t;
-        key[t] = ~0ull;
-        if (s < c0 + c1) {
-            const int32_t j = s < c0 ? cand_ids[(q * 2) * cap + s]
-                                     : cand_ids[(q * 2 + 1) * cap + (s - c0)];
-            const float dd = exact_d2(xr, x + (int64_t)j * d, d);
-            key[t] = ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
-        }
+        int32_t j = -1;
+        if (s < c0 + c1)
+            j = s < c0 ? cand_ids[(q * 2) * cap + s] : cand_ids[(q * 2 + 1) * cap + (s - c0)];
+        // every lane joins the staging (it is warp-wide), the rounds are uniform per warp
+        const float dd = t * 32 < c0 + c1 ? staged_d2(x, d, q_s, j, rows_s, lane) : CUSCAN_INF;
+        key[t] = j < 0 ? ~0ull : ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
     }
     for (int r = 0; r < k; ++r) {
         unsigned long long mine = key[0];
@@ -1016,15 +1052,25 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
         }
         return;
     }
-    const float *xr = xp + pos * d;
+    if (c0 + c1 == 0) return;  // no candidate: the row keeps an empty key
+    extern __shared__ float rerank_smem[];
+    float *q_s = rerank_smem + (threadIdx.x >> 5) * rerank_warp_floats(d);
+    float *rows_s = q_s + d;
+    for (int f = lane; f < d; f += 32) q_s[f] = xp[pos * d + f];
+    __syncwarp();
     const float ci = corep[pos];
     const int32_t li = labp[pos];
     unsigned long long mine = ~0ull;
-    for (int s = lane; s < c0 + c1; s += 32) {
-        const int32_t j = s < c0 ? cand_ids[(pos * 2) * cap + s]
-                                 : cand_ids[(pos * 2 + 1) * cap + (s - c0)];
-        if (labp[j] == li) continue;
-        const float w = fmaxf(fmaxf(exact_d2(xr, xp + (int64_t)j * d, d), ci), corep[j]);
+    for (int base = 0; base < c0 + c1; base += 32) {
+        const int s = base + lane;
+        int32_t j = -1;
+        if (s < c0 + c1) {
+            j = s < c0 ? cand_ids[(pos * 2) * cap + s] : cand_ids[(pos * 2 + 1) * cap + (s - c0)];
+            if (labp[j] == li) j = -1;
+        }
+        const float d2 = staged_d2(xp, d, q_s, j, rows_s, lane);
+        if (j < 0) continue;
+        const float w = fmaxf(fmaxf(d2, ci), corep[j]);
         if (w != w) continue;
         const unsigned long long key =
             ((unsigned long long)weight_key_bits(w) << 32) | (uint32_t)perm[j];
@@ -1359,7 +1405,10 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     constexpr int M = 32;
     if ((rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xs, perm, n, d,
+    const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
+    if ((rc = allow_dynamic_smem(ctx, rerank_knn_kernel<M>, rr_smem))) return rc;
+    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
+                  32 * RERANK_WARPS, rr_smem, s, xs, perm, n, d,
                   k, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
                   as<int32_t>(R.fallback), as<float>(R.qthr), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
@@ -1396,7 +1445,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
                                                    nullptr, s, nullptr, Q)))
             return rc;
         CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-        CUSCAN_KERNEL(rerank_knn_threshold_kernel, (unsigned)ceil_div(nq * 32, 256), 256, 0, s, xs,
+        if ((rc = allow_dynamic_smem(ctx, rerank_knn_threshold_kernel, rr_smem))) return rc;
+        CUSCAN_KERNEL(rerank_knn_threshold_kernel, (unsigned)ceil_div(nq, (int64_t)RERANK_WARPS),
+                      32 * RERANK_WARPS, rr_smem, s, xs,
                       perm, as<int32_t>(R.fallback), nq, d, k, as<int32_t>(R.cand2),
                       as<int32_t>(R.rowcnt2), KNN_CAP, ids, dist, as<int32_t>(R.fallback2),
                       as<int>(R.count));
@@ -1446,7 +1497,10 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     constexpr int M = 32;
     if ((rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n * 32, 256), 256, 0, s, xp, corep,
+    const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
+    if ((rc = allow_dynamic_smem(ctx, rerank_boruvka_kernel, rr_smem))) return rc;
+    CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
+                  32 * RERANK_WARPS, rr_smem, s, xp, corep,
                   labp, perm, n, d, as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
                   row_keys, as<int32_t>(R.fallback), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
