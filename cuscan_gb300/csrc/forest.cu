@@ -525,7 +525,8 @@ int forest_buffers(ForestBuffers &b, Buffer **out) {
                      &b.knn_dist_tmp, &r.xt, &r.pnorm, &r.mnorm, &r.tile_mmax, &r.tile_lo,
                      &r.tile_hi, &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
                      &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d, &r.absmax,
-                     &r.qthr, &r.xq, &r.pq, &r.mq, &r.cand2, &r.rowcnt2, &r.fallback2};
+                     &r.qthr, &r.xq, &r.pq, &r.mq, &r.cand2, &r.rowcnt2, &r.fallback2,
+                     &r.urow, &r.colcnt, &r.colbuf};
     static_assert(sizeof(all) / sizeof(all[0]) == kForestBufferCount, "buffer list");
     const int count = (int)(sizeof(all) / sizeof(all[0]));
     if (out)

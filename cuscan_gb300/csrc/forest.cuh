@@ -19,6 +19,7 @@ struct RefinedBuffers {
     Buffer xt, pnorm, mnorm, tile_mmax, tile_lo, tile_hi, cand_ids, cand_lb, fallback, count;
     Buffer error, cbound, rowcnt, pivots, cells, cell_d, absmax;
     Buffer qthr, xq, pq, mq, cand2, rowcnt2, fallback2;  // threshold re-screen of kNN rows
+    Buffer urow, colcnt, colbuf;  // symmetric Borůvka: row bounds, column-side buffers
     // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
     bool want_fp16 = false;  // requested by the caller's precision
     bool fp16 = false;       // in use (the data's range allows a scale)
@@ -43,7 +44,7 @@ struct ForestBuffers {
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
 void forest_release(ForestBuffers &b);
 // Every device buffer of the forest and of the bf16 screen (out may be null); returns the count.
-constexpr int kForestBufferCount = 52;
+constexpr int kForestBufferCount = 55;
 int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);

@@ -75,12 +75,25 @@ struct Params {
     int64_t nq;               // query rows
     const int32_t *qpos;      // position of each query row in the reference order (null: same)
     const float *qthr;        // threshold mode: per-query upper bound of the k-th distance (raw)
+    // symmetric Borůvka: per-row upper bounds of the cheapest cross edge (raw f32 bits) and the
+    // per-row buffers that other query blocks append column-side pairs to
+    uint32_t *urow;
+    int32_t *colcnt;
+    int32_t *colbuf;
+    int capc;
 };
 
 // Screen modes: kNN lists, Borůvka thresholds with shared component bounds, kNN thresholds.
 constexpr int MODE_KNN_LIST = 0;
 constexpr int MODE_BORUVKA = 1;
 constexpr int MODE_KNN_THRESHOLD = 2;
+// Borůvka over each unordered pair once: a query block visits its own tile (both halves see
+// every pair inside it) and the tiles after it, testing each pair for its row and, through
+// the column-side buffers, for its column.
+constexpr int MODE_BORUVKA_SYM = 3;
+constexpr int BORUVKA_COL_CAP = 64;  // column-side candidate slots per row
+constexpr double SYM_UNBOUNDED_MAX = 0.25;  // largest share of unbounded rows for the symmetric screen
+constexpr int64_t SYM_MIN_ROWS = 131072;     // smallest point set for the symmetric screen
 constexpr int KNN_CAP = 128;  // threshold-mode candidate slots per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
@@ -304,6 +317,21 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
     return r;
 }
 
+// Order-preserving map of f32 values to u32 (for integer warp reductions) and back.
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+    return ord2f(__reduce_max_sync(0xffffffffu, f2ord(v)));
+}
+__device__ __forceinline__ float warp_min_f(float v) {
+    return ord2f(__reduce_min_sync(0xffffffffu, f2ord(v)));
+}
+
 // Largest of 32 values with three-input maxima.
 __device__ __forceinline__ float max32(const float (&v)[32]) {
     float t[12];
@@ -329,6 +357,24 @@ __device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_
     if (i < w) return a + i;
     const int64_t j = i - w;
     return j < a ? j : j + w;
+}
+
+// Tiles query block qb visits and the i-th of them. The symmetric Borůvka mode visits the
+// block's own tile and then every later tile in order; the other modes visit every tile
+// (tile_order).
+template <bool SYM>
+__device__ __forceinline__ int64_t vis_count(const Params &P, int64_t qb) {
+    return SYM ? P.n_tiles - (qb >> 1) : P.n_tiles;
+}
+template <bool SYM>
+__device__ __forceinline__ int64_t vis_tile(const Params &P, int64_t qb, int64_t wa, int64_t i) {
+    return SYM ? (qb >> 1) + i : tile_order(P, wa, i);
+}
+
+// The query block a CTA takes at its qi-th step (blocks in order, strided over the CTAs).
+template <bool SYM>
+__device__ __forceinline__ int64_t block_at(const Params &P, int64_t qi) {
+    return qi;
 }
 
 // Label range of query block qb (4 chunks of 32 rows).
@@ -368,7 +414,8 @@ __device__ __forceinline__ void list_insert(float (&L)[M], int (&J)[M], float x,
 
 template <int M, int MODE>
 __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
-    constexpr bool BORUVKA = MODE == MODE_BORUVKA;
+    constexpr bool BORUVKA = MODE == MODE_BORUVKA || MODE == MODE_BORUVKA_SYM;
+    constexpr bool SYM = MODE == MODE_BORUVKA_SYM;
     constexpr bool THRESH = MODE == MODE_KNN_THRESHOLD;
     constexpr bool APPEND = BORUVKA || THRESH;  // threshold modes append to per-row buffers
     extern __shared__ uint8_t smem_raw[];
@@ -426,7 +473,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             // parity of the last fill of each stage (bit 1 set = a fill was issued)
             uint32_t issued[4] = {0, 0, 0, 0};
             uint32_t a_issued = 0;
-            for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
+                const int64_t qb = block_at<SYM>(P, qi);
                 if (!mbar_wait(a_empty, a_phase ^ 1, abort, P.error)) break;
                 a_issued = 2u | a_phase;
                 a_phase ^= 1;
@@ -438,8 +486,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
-                for (int64_t i = 0; i < P.n_tiles; ++i) {
-                    const int64_t t = tile_order(P, wa, i);
+                const int64_t nvis = vis_count<SYM>(P, qb);
+                for (int64_t i = 0; i < nvis; ++i) {
+                    const int64_t t = vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
                     issued[stage] = 2u | phase;
@@ -474,16 +523,18 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             uint32_t phase = 0, a_phase = 0;
             uint32_t tcount = 0, a_commits = 0;
             const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
-            for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
+                const int64_t qb = block_at<SYM>(P, qi);
                 if (!mbar_wait(a_full, a_phase, abort, P.error)) break;
                 a_phase ^= 1;
                 fence_after();
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
+                const int64_t nvis = vis_count<SYM>(P, qb);
                 bool ok = true;
-                for (int64_t i = 0; i < P.n_tiles; ++i) {
-                    const int64_t t = tile_order(P, wa, i);
+                for (int64_t i = 0; i < nvis; ++i) {
+                    const int64_t t = vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                     if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
@@ -532,7 +583,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
         const bool debug = P.debug_tile != nullptr && blockIdx.x == 0;
         uint32_t tcount = 0;
-        for (int64_t qb = blockIdx.x; qb < P.n_qblocks && !*abort; qb += gridDim.x) {
+        for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
+            const int64_t qb = block_at<SYM>(P, qi);
             const int64_t row = qb * BM + row_local;  // query row
             const bool valid = row < P.nq;
             const int64_t self = valid && P.qpos ? (int64_t)P.qpos[row] : row;
@@ -567,9 +619,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
             const int64_t wa = window_start(P, qb);
+            const int64_t nvis = vis_count<SYM>(P, qb);
+            // symmetric mode: the warp's 32 rows summarised for the column-side block test
+            float psmin_w = CUSCAN_INF, cmmax_w = 0.0f, coremin_w = CUSCAN_INF;
+            if (SYM) {
+                psmin_w = warp_min_f(valid ? ps_i : CUSCAN_INF);
+                cmmax_w = warp_max_f(valid ? cm_i : 0.0f);
+                coremin_w = warp_min_f(valid ? core_i : CUSCAN_INF);
+            }
             // next visited position i (>= i0) in this block's tile order
             auto next_index = [&](int64_t i) -> int64_t {
-                while (i < P.n_tiles && tile_skipped<BORUVKA>(P, tile_order(P, wa, i), qlo, qhi)) ++i;
+                while (i < nvis && tile_skipped<BORUVKA>(P, vis_tile<SYM>(P, qb, wa, i), qlo, qhi)) ++i;
                 return i;
             };
             // per-tile column data, fetched one tile ahead
@@ -577,6 +637,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             float4 pre_m = make_float4(0, 0, 0, 0);
             int32_t pre_ch = -2;
             float pre_mt = 0.0f, pre_cb = CUSCAN_INF;
+            float4 pre_t = make_float4(0, 0, 0, 0);  // symmetric mode: column row bounds (raw)
             auto prefetch = [&](int64_t t) {
                 const int64_t col = t * BN + half * HALF + lane * 4;
                 pre_p = *reinterpret_cast<const float4 *>(P.pnorm + col);
@@ -597,13 +658,20 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
                     pre_cb = valid ? __uint_as_float(*(volatile uint32_t *)&P.cbound[lab_i])
                                    : CUSCAN_INF;
+                    if (SYM) {
+                        const volatile uint32_t *ur = P.urow;
+                        pre_t.x = col + 0 < P.n ? __uint_as_float(ur[col + 0]) : -CUSCAN_INF;
+                        pre_t.y = col + 1 < P.n ? __uint_as_float(ur[col + 1]) : -CUSCAN_INF;
+                        pre_t.z = col + 2 < P.n ? __uint_as_float(ur[col + 2]) : -CUSCAN_INF;
+                        pre_t.w = col + 3 < P.n ? __uint_as_float(ur[col + 3]) : -CUSCAN_INF;
+                    }
                 }
             };
             int64_t ti = next_index(0);
-            if (ti < P.n_tiles) prefetch(tile_order(P, wa, ti));
+            if (ti < nvis) prefetch(vis_tile<SYM>(P, qb, wa, ti));
             bool ok = true;
-            while (ti < P.n_tiles) {
-                const int64_t t = tile_order(P, wa, ti);
+            while (ti < nvis) {
+                const int64_t t = vis_tile<SYM>(P, qb, wa, ti);
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
@@ -637,11 +705,21 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         reinterpret_cast<float2 *>(my_pb + 6 * HALF + b * 8)[lane >> 3] =
                             make_float2(pmin, cmin);
                 }
+                // symmetric mode: the largest column row bound of each chunk (scaled)
+                float chunk_tmax[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (SYM) {
+                    float tm = fmaxf(fmaxf(pre_t.x, pre_t.y), fmaxf(pre_t.z, pre_t.w)) * P.s2;
+#pragma unroll
+                    for (int o = 1; o < 8; o <<= 1)
+                        tm = fmaxf(tm, __shfl_xor_sync(0xffffffffu, tm, o));
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) chunk_tmax[c] = __shfl_sync(0xffffffffu, tm, 8 * c);
+                }
                 const float mt = pre_mt;
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
-                if (ti_next < P.n_tiles) prefetch(tile_order(P, wa, ti_next));
+                if (ti_next < nvis) prefetch(vis_tile<SYM>(P, qb, wa, ti_next));
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -721,6 +799,72 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     }
                 }
                 const unsigned warp_bits = __reduce_or_sync(0xffffffffu, hitbits);
+                // Symmetric mode, tiles after the block's own: the pairs of this block are also
+                // the pairs of the tile's rows. Block test: with the warp's smallest scaled norm
+                // and core and largest C_A m, the chunk's smallest scaled norm and core and the
+                // block's largest dot product, fmaf/add rounding being monotonic, wl is below
+                // every pair's exact-path bound max(lb, core_i, core_j); only blocks where it
+                // reaches a column's row bound are tested pair by pair.
+                unsigned colbits = 0;
+                if (SYM && t > (qb >> 1)) {
+#pragma unroll
+                    for (int c = 0; c < HALF / 32; ++c) {
+                        const float vb = warp_max_f(vmax[c]);
+                        const float2 cmn = chunk_min[c];
+                        const float lbb = fmaf(-cmmax_w, mt, fmaf(-2.0f, vb, cmn.x) + psmin_w);
+                        const float wl = fmaxf(fmaxf(lbb, coremin_w), cmn.y);
+                        if (wl <= chunk_tmax[c]) colbits |= 1u << c;
+                    }
+                }
+                for (int c = 0; colbits != 0 && c < HALF / 32; ++c) {
+                    if (!((colbits >> c) & 1u)) continue;
+                    uint32_t rc2[32];
+                    tmem_ld32_issue(taddr + c * 32, rc2);
+                    // lane e refreshes column e's row bound with its component's current bound
+                    // (rows of components that found edges elsewhere get tight at once)
+                    const int64_t j0 = t * BN + half * HALF + c * 32;
+                    int32_t lab_l = -1;
+                    float t_l = -CUSCAN_INF;
+                    if (j0 + lane < P.n) {
+                        lab_l = P.label[j0 + lane];
+                        const uint32_t cbv = *(volatile uint32_t *)&P.cbound[lab_l];
+                        const uint32_t old = atomicMin(&P.urow[j0 + lane], cbv);
+                        t_l = __uint_as_float(old < cbv ? old : cbv) * P.s2;
+                    }
+                    tmem_ld_wait(rc2);
+#pragma unroll
+                    for (int e = 0; e < 32; ++e) {
+                        const float tj = __shfl_sync(0xffffffffu, t_l, e);
+                        const int32_t lab_j = __shfl_sync(0xffffffffu, lab_l, e);
+                        const int col = c * 32 + e;
+                        const int64_t j = j0 + e;
+                        if (j >= P.n) break;  // the same for every lane
+                        const float lb = fmaf(-cm_i, mb[col],
+                                              fmaf(-2.0f, __uint_as_float(rc2[e]), pb[col]) + ps_i);
+                        const float cj = cb[col];
+                        const float lbw = fmaxf(fmaxf(lb, core_i), cj);
+                        const bool pv = valid && lab_j != lab_i && lbw <= tj;
+                        const float eps2 =
+                            2.0f * fmaf(cm_i, mb[col], P.c_b * (ps_i + pb[col]) * 1.001f) +
+                            4.0f * P.abs_c;
+                        const float ubr = lb + eps2;
+                        const float ub =
+                            fmaxf(fmaxf(ubr + 0x1p-20f * (fabsf(ubr) + eps2), core_i), cj);
+                        // the block's best upper bound for this column's row: a pair above
+                        // it cannot be the row's cheapest edge
+                        const float tmin = warp_min_f(pv ? ub : CUSCAN_INF);
+                        if (pv && lbw <= tmin) {
+                            const int slot = atomicAdd(&P.colcnt[j], 1);
+                            if (slot < P.capc) P.colbuf[j * P.capc + slot] = (int32_t)row;
+                        }
+                        if (lane == 0 && tmin < CUSCAN_INF) {
+                            const uint32_t ub_raw = __float_as_uint(__fmul_ru(tmin, P.inv_s2));
+                            atomicMin(&P.urow[j], ub_raw);
+                            atomicMin(&P.cbound[lab_j], ub_raw);
+                        }
+                    }
+                    __syncwarp();
+                }
                 for (int c = 0; warp_bits != 0 && c < HALF / 32; ++c) {
                     if (!((warp_bits >> c) & 1u)) continue;
                     uint32_t rc_[32];
@@ -812,7 +956,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 if (lane == 0) mbar_arrive(&t_empty[b]);
                 if (BORUVKA && valid && U < published) {
                     // raw units, rounded up so that the bound stays an upper bound
-                    atomicMin(&P.cbound[lab_i], __float_as_uint(__fmul_ru(U, P.inv_s2)));
+                    const uint32_t u_raw = __float_as_uint(__fmul_ru(U, P.inv_s2));
+                    atomicMin(&P.cbound[lab_i], u_raw);
+                    if (SYM) atomicMin(&P.urow[row], u_raw);
                     published = U;
                 }
                 ++tcount;
@@ -1038,6 +1184,8 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
                                       const int32_t *__restrict__ perm, int64_t n, int d,
                                       const int32_t *__restrict__ cand_ids,
                                       const int32_t *__restrict__ rowcnt, int cap,
+                                      const int32_t *__restrict__ colcnt,
+                                      const int32_t *__restrict__ colbuf, int capc,
                                       unsigned long long *__restrict__ row_keys,
                                       int32_t *__restrict__ fallback,
                                       int *__restrict__ fallback_count) {
@@ -1045,14 +1193,16 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
     const int lane = threadIdx.x & 31;
     if (pos >= n) return;
     const int c0 = rowcnt[pos * 2], c1 = rowcnt[pos * 2 + 1];
-    if (c0 > cap || c1 > cap) {
+    const int c2 = colcnt ? colcnt[pos] : 0;  // pairs other blocks appended for this row
+    if (c0 > cap || c1 > cap || c2 > capc) {
         if (lane == 0) {
             const int at = atomicAdd(fallback_count, 1);
             fallback[at] = (int32_t)pos;
         }
         return;
     }
-    if (c0 + c1 == 0) return;  // no candidate: the row keeps an empty key
+    const int total = c0 + c1 + c2;
+    if (total == 0) return;  // no candidate: the row keeps an empty key
     extern __shared__ float rerank_smem[];
     float *q_s = rerank_smem + (threadIdx.x >> 5) * rerank_warp_floats(d);
     float *rows_s = q_s + d;
@@ -1061,11 +1211,13 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
     const float ci = corep[pos];
     const int32_t li = labp[pos];
     unsigned long long mine = ~0ull;
-    for (int base = 0; base < c0 + c1; base += 32) {
+    for (int base = 0; base < total; base += 32) {
         const int s = base + lane;
         int32_t j = -1;
-        if (s < c0 + c1) {
-            j = s < c0 ? cand_ids[(pos * 2) * cap + s] : cand_ids[(pos * 2 + 1) * cap + (s - c0)];
+        if (s < total) {
+            j = s < c0        ? cand_ids[(pos * 2) * cap + s]
+                : s < c0 + c1 ? cand_ids[(pos * 2 + 1) * cap + (s - c0)]
+                              : colbuf[pos * capc + (s - c0 - c1)];
             if (labp[j] == li) j = -1;
         }
         const float d2 = staged_d2(xp, d, q_s, j, rows_s, lane);
@@ -1108,6 +1260,22 @@ __global__ void pick_pivots_kernel(const float *__restrict__ x, int64_t n, int d
     const int f = (int)(e - p * d);
     const int64_t r = (p * n) / npiv;
     piv[e] = x[r * d + f];
+}
+
+// Per-row bounds of the symmetric screen: the bound of the row's component.
+// Also counts the rows whose component has no bound yet.
+__global__ void init_row_bounds_kernel(const uint32_t *__restrict__ cbound,
+                                       const int32_t *__restrict__ labp, int64_t n,
+                                       uint32_t *__restrict__ urow, int *__restrict__ unbounded) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool inf = false;
+    if (i < n) {
+        const uint32_t b = cbound[labp[i]];
+        urow[i] = b;
+        inf = b >= 0x7f800000u;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, inf);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(unbounded, __popc(m));
 }
 
 __global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
@@ -1200,6 +1368,8 @@ size_t refined_workspace_bytes(int64_t n, int d, int k) {
     // candidates, counts, fallback list
     b += 4 * (size_t)n + (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;
     b += 4 * (size_t)n * 2 * KNN_CAP + 8 * (size_t)n + 4 * (size_t)n;
+    // symmetric Borůvka: row bounds, column-side counts and candidates
+    b += 8 * (size_t)n + 4 * (size_t)n * BORUVKA_COL_CAP;
     return b;
 }
 
@@ -1292,7 +1462,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
                       const float *core, const int32_t *label, const int32_t *chunk_lo,
                       const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr,
                       const QuerySet &Q = QuerySet()) {
-    constexpr bool BORUVKA = MODE == MODE_BORUVKA;
+    constexpr bool BORUVKA = MODE == MODE_BORUVKA || MODE == MODE_BORUVKA_SYM;
     int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * 2 * M, "screen candidates");
     if (!rc) rc = ensure(ctx, R.cand_lb, sizeof(float) * n * 2 * M, "screen bounds");
     if (rc) return rc;
@@ -1341,6 +1511,12 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         P.cbound = as<uint32_t>(R.cbound);
         P.rowcnt = as<int32_t>(R.rowcnt);
         CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowcnt.ptr, 0, sizeof(int32_t) * 2 * n, s));
+    }
+    if (MODE == MODE_BORUVKA_SYM) {
+        P.urow = as<uint32_t>(R.urow);
+        P.colcnt = as<int32_t>(R.colcnt);
+        P.colbuf = as<int32_t>(R.colbuf);
+        P.capc = BORUVKA_COL_CAP;
     }
     if (MODE == MODE_KNN_THRESHOLD) {
         P.cap = KNN_CAP;
@@ -1493,16 +1669,42 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                   0x7f800000u);
     CUSCAN_KERNEL(seed_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, knn_ids, knn_sq, k,
                   core, label, n, as<uint32_t>(R.cbound));
+    // symmetric screen: per-row bounds start at the component bounds; empty column buffers
+    if ((rc = ensure(ctx, R.urow, sizeof(uint32_t) * n, "row bounds"))) return rc;
+    if ((rc = ensure(ctx, R.colcnt, sizeof(int32_t) * n, "column-side counts"))) return rc;
+    if ((rc = ensure(ctx, R.colbuf, sizeof(int32_t) * n * BORUVKA_COL_CAP, "column-side candidates")))
+        return rc;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.colcnt.ptr, 0, sizeof(int32_t) * n, s));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+    CUSCAN_KERNEL(init_row_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
+                  as<uint32_t>(R.cbound), labp, n, as<uint32_t>(R.urow), as<int>(R.count));
+    CUSCAN_LAUNCH(ctx, "init_row_bounds_kernel");
+    // The symmetric screen halves the tensor-core and epilogue work but tests a pair for its
+    // column's row only against that row's known bound; rows of components without a bound
+    // draw many appends there. Small sets (where fixed costs dominate) and rounds with many
+    // unbounded rows run the one-sided screen.
+    bool sym = n >= SYM_MIN_ROWS;
+    if (sym) {
+        int unbounded = 0;
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(&unbounded, R.count.ptr, sizeof(int),
+                                         cudaMemcpyDeviceToHost, s));
+        CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+        sym = (double)unbounded <= SYM_UNBOUNDED_MAX * (double)n;
+    }
     CUSCAN_LAUNCH(ctx, "component bounds");
     constexpr int M = 32;
-    if ((rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s))) return rc;
+    if (sym) rc = run_screen<M, MODE_BORUVKA_SYM>(ctx, R, L, n, d, corep, labp, clo, chi, s);
+    else rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s);
+    if (rc) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
     if ((rc = allow_dynamic_smem(ctx, rerank_boruvka_kernel, rr_smem))) return rc;
     CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
                   32 * RERANK_WARPS, rr_smem, s, xp, corep,
                   labp, perm, n, d, as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
-                  row_keys, as<int32_t>(R.fallback), as<int>(R.count));
+                  sym ? as<int32_t>(R.colcnt) : nullptr, as<int32_t>(R.colbuf), BORUVKA_COL_CAP,
+                  row_keys,
+                  as<int32_t>(R.fallback), as<int>(R.count));
     CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
     int fallbacks = 0;
     if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;

@@ -193,8 +193,9 @@ def test_threshold_rescreen_matches_oracle(gpu_ctx, precision):
 
 
 def test_full_size_refined_equals_plain(gpu_ctx):
-    """vmf_500k_d128 reduced to n=120000: bf16-refined and plain fits agree bit for bit."""
-    x, ms, _ = synthetic.workload("vmf_500k_d128", n=120000)
+    """vmf_500k_d128 reduced to n=150000 (large enough for the symmetric Borůvka screen):
+    bf16-refined and plain fits agree bit for bit."""
+    x, ms, _ = synthetic.workload("vmf_500k_d128", n=150000)
     a = gpu_ctx.fit_core(x, ms, _lib.PRECISION_PLAIN)
     b = gpu_ctx.fit_core(x, ms, _lib.PRECISION_BF16_REFINED)
     for key in ("knn_ids", "src", "dst"):
@@ -202,3 +203,16 @@ def test_full_size_refined_equals_plain(gpu_ctx):
     for key in ("knn_sq", "core_sq", "wsq"):
         np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
     check_tree_properties(x, b, ms)
+
+
+def test_large_blobs_fp16_equals_plain(gpu_ctx):
+    """Gaussian blobs far from the origin at n=140000 (symmetric screen where the rows have
+    bounds, one-sided rounds where many do not): fp16-refined and plain agree bit for bit."""
+    x = synthetic.gaussian_mixture(140000, 32, 30, seed=140032)
+    a = gpu_ctx.fit_core(x, 5, _lib.PRECISION_PLAIN)
+    b = gpu_ctx.fit_core(x, 5, _lib.PRECISION_FP16_REFINED)
+    for key in ("knn_ids", "src", "dst"):
+        np.testing.assert_array_equal(a[key], b[key])
+    for key in ("knn_sq", "core_sq", "wsq"):
+        np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
+    check_tree_properties(x, b, 5)
