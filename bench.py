@@ -147,11 +147,14 @@ def measured_peaks():
 
 # DRAM bytes per launch of the dominant kernel (mean over the Borůvka screen launches of one
 # fit), from the one-pass ncu capture summarised in profiles/screen_dram_vmf500k_d128.md.
-NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": 82314801216.0}
+NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": 1783891968.0}
 
 
-def ncu_traffic(workload: str, precision: str):
-    """DRAM bytes per launch of the dominant kernel measured by ncu for this workload, if any."""
+def ncu_traffic(workload: str, precision: str, n_override):
+    """DRAM bytes per launch of the dominant kernel measured by ncu for this workload (at its
+    own size), if any."""
+    if n_override is not None:
+        return None
     return NCU_TRAFFIC.get(f"{workload}:{precision}")
 
 
@@ -616,10 +619,18 @@ def run_ours(args):
         achieved, t_dom, w_dom = w_cand / t_cand / 1e12, t_cand, w_cand
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": bf16_peak,
             "unit": "TFLOP/s", "frac": achieved / bf16_peak, "peak_source": f"{peak_src} bf16",
-            "traffic": ncu_traffic(args.workload, args.precision),
+            "traffic": ncu_traffic(args.workload, args.precision, args.n),
             "kernel_ms": t_dom * 1e3, "algorithmic_tflop": w_dom / 1e12}
     if roof["traffic"] is not None:
         roof["traffic_scope"] = "ncu dram read+write bytes, mean per Borůvka screen launch"
+    if args.precision != "fp32":
+        d_pad = -(-d // 64) * 64
+        tiles = int(stats["screen_tile_pairs"])
+        roof["tensor_tiles"] = tiles
+        roof["tensor_tflop_executed"] = tiles * 2.0 * 128 * 256 * d_pad / 1e12
+        roof["work_note"] = ("achieved counts the algorithmic work (every ordered cross pair, "
+                             "no credit for the symmetric screen); tensor_tflop_executed is what "
+                             "the screens ran on the tensor cores over the whole fit")
     if args.precision == "fp32":
         roof["note"] = ("plain form runs f32 direct differences on the SIMT pipes; the fraction "
                         "is against the measured bf16 tensor peak")

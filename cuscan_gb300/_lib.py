@@ -104,6 +104,7 @@ class FitStats(C.Structure):
         ("boruvka_fallback_rows", C.c_int64),
         ("cross_pairs", C.c_double),
         ("rescreened_rows", C.c_int64),
+        ("screen_tile_pairs", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -259,6 +259,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0, rescreened_rows = 0;
     b.refined.want_fp16 = precision == CUSCAN_PRECISION_FP16_REFINED;
     b.refined.have_scale = false;
+    b.refined.tile_pairs = 0;
 
     CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
@@ -328,6 +329,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->boruvka_fallback_rows = boruvka_fallback_rows;
         stats->cross_pairs = cross_pairs;
         stats->rescreened_rows = rescreened_rows;
+        stats->screen_tile_pairs = b.refined.tile_pairs;
     }
     return CUSCAN_OK;
 }

@@ -25,6 +25,7 @@ struct RefinedBuffers {
     bool fp16 = false;       // in use (the data's range allows a scale)
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;
+    int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
 };
 
 struct ForestBuffers {

@@ -59,7 +59,7 @@ struct Params {
     float c_a, one_minus_cb;
     int32_t *cand_ids;        // [n][M]
     float *cand_lb;           // [n][M]
-    int *error;
+    int *error;               // [0]: error flag; bytes 8..15: (qb, tile) pairs the MMA ran (u64)
     float *debug_tile;        // when set: CTA 0 writes its first raw 128 x 256 accumulator tile
     float c_b;                // norm coefficient of the bound (upper bounds use it)
     uint32_t *cbound;         // Borůvka: per-component upper bound of the cheapest edge (f32 bits)
@@ -563,6 +563,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 ++a_commits;
                 if (!ok) break;
             }
+            atomicAdd(reinterpret_cast<unsigned long long *>(P.error + 2),
+                      (unsigned long long)tcount);
             // wait until every issued MMA has completed before TMEM can be released
             mma_commit(done);
             for (uint32_t it = 0; it < WAIT_POLLS; ++it)
@@ -1524,7 +1526,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         P.rowcnt = Q.rowcnt;
     }
     if (P.n_qblocks == 0) return CUSCAN_OK;
-    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, sizeof(int), s));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, 16, s));
     auto kernel = screen_kernel<M, MODE>;
     if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
     int64_t grid = P.n_qblocks < ctx->sm_count ? P.n_qblocks : ctx->sm_count;
@@ -1534,14 +1536,17 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
 }
 
 static int read_screen_status(cuscan_ctx *ctx, RefinedBuffers &R, cudaStream_t s, int &fallbacks) {
-    int host[2] = {0, 0};
-    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&host[0], R.error.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&host[1], R.count.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    unsigned long long status[2] = {0, 0};  // error flag, tile pairs
+    int count = 0;
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(status, R.error.ptr, 16, cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&count, R.count.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
-    if (host[0])
+    if ((int)(status[0] & 0xffffffffu))
         return fail(ctx, CUSCAN_BACKEND_UNAVAILABLE,
                     "tensor-core screening timed out waiting on a pipeline barrier");
-    fallbacks = host[1];
+    R.tile_pairs += (int64_t)status[1];
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, 16, s));
+    fallbacks = count;
     return CUSCAN_OK;
 }
 

@@ -83,6 +83,7 @@ typedef struct cuscan_fit_stats {
     int64_t boruvka_fallback_rows; /* Borůvka rows (summed over rounds) re-run exact f32 */
     double cross_pairs;      /* sum over rounds of ordered cross-component pairs */
     int64_t rescreened_rows; /* kNN rows screened a second time in threshold mode */
+    int64_t screen_tile_pairs; /* 128 x 256 tensor-core tiles the screens computed */
 } cuscan_fit_stats;
 
 /* ---- context ---- */
