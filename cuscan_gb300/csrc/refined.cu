@@ -94,7 +94,7 @@ constexpr int MODE_BORUVKA_SYM = 3;
 constexpr int BORUVKA_COL_CAP = 64;  // column-side candidate slots per row
 constexpr double SYM_UNBOUNDED_MAX = 0.25;  // largest share of unbounded rows for the symmetric screen
 constexpr int64_t SYM_MIN_ROWS = 131072;     // smallest point set for the symmetric screen
-constexpr int KNN_CAP = 128;  // threshold-mode candidate slots per row half
+constexpr int KNN_CAP = 512;  // threshold-mode candidate slots per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
 // ---- PTX wrappers ----
