@@ -84,6 +84,12 @@ SIGNATURES = {
     "cuscan_server_read_predict": (C.c_int, [_VP, C.c_int64, _VP, _VP, _VP]),
     "cuscan_predictor_shape": (C.c_int, [_VP, _I64P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "cuscan_predict_workspace_bytes": (C.c_int64, [_VP, C.c_int64]),
+    "cuscan_predictor_state_shape": (C.c_int, [_VP, _I64P, _I64P]),
+    "cuscan_predictor_export": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                          _VP]),
+    "cuscan_predictor_from_state": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, _VP,
+                                              C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                              C.POINTER(_VP), C.c_char_p, C.c_size_t]),
     "cuscan_server_request_error": (C.c_int, [_VP, C.c_int64, C.c_char_p, C.c_size_t]),
     "cuscan_server_release": (C.c_int, [_VP, C.c_int64]),
     "cuscan_server_get_stats": (C.c_int, [_VP, _VP]),

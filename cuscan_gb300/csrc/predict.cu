@@ -406,6 +406,224 @@ void cuscan_predictor_destroy(cuscan_predictor *p) {
     delete p;
 }
 
+// ---- portable state (crates/hdbscan-core/src/prediction.rs:161-433) ----
+
+int cuscan_predictor_state_shape(const cuscan_predictor *p, int64_t *n_finite,
+                                 int64_t *cluster_nodes) {
+    if (!p) return CUSCAN_INVALID_INPUT;
+    const bool tree = !p->node_id.empty();
+    if (n_finite) *n_finite = tree ? p->n_finite : 0;
+    if (cluster_nodes) *cluster_nodes = (int64_t)p->node_id.size();
+    return CUSCAN_OK;
+}
+
+int cuscan_predictor_export(cuscan_ctx *ctx, const cuscan_predictor *p, float *geometry,
+                            uint32_t *finite_index, uint64_t *node_ids,
+                            uint64_t *node_parent_indices, double *node_birth_lambdas,
+                            int32_t *node_labels, double *node_max_lambdas,
+                            uint64_t *point_node_indices, double *point_departure_lambdas,
+                            double *prediction_cores) {
+    if (!p) return CUSCAN_INVALID_INPUT;
+    if (p->node_id.empty()) return CUSCAN_OK;  // no-cluster-tree state: nothing to export
+    cuscan_ctx local;
+    cuscan_ctx *ectx = ctx ? ctx : &local;
+    if (!finite_index || !node_ids || !node_parent_indices || !node_birth_lambdas ||
+        !node_labels || !node_max_lambdas || !point_node_indices || !point_departure_lambdas ||
+        !prediction_cores)
+        return fail(ectx, CUSCAN_INVALID_INPUT, "predictor export received a null pointer");
+    clear_error(ectx);
+    // A host-only predictor (no device rows) exports its columns without geometry.
+    if (p->train) {
+        if (!ctx || !geometry)
+            return fail(ectx, CUSCAN_INVALID_INPUT, "predictor geometry export needs a context "
+                        "and a buffer");
+        if (p->device != ctx->device)
+            return fail(ctx, CUSCAN_INVALID_INPUT, "the predictor's training rows are not on this "
+                        "device");
+        CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(geometry, p->train, sizeof(float) * p->n_finite * p->d,
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+    } else if (geometry) {
+        return fail(ectx, CUSCAN_INVALID_INPUT, "this predictor holds no training rows");
+    }
+    const size_t nn = p->node_id.size();
+    for (size_t i = 0; i < nn; ++i) {
+        node_ids[i] = (uint64_t)p->node_id[i];
+        node_parent_indices[i] = p->node_parent[i] < 0 ? UINT64_MAX : (uint64_t)p->node_parent[i];
+        node_birth_lambdas[i] = p->node_birth[i];
+        node_labels[i] = p->node_label[i];
+        node_max_lambdas[i] = p->node_max[i];
+    }
+    for (int64_t i = 0; i < p->n_finite; ++i) {
+        finite_index[i] = p->finite_index[i];
+        point_node_indices[i] = (uint64_t)p->point_node[i];
+        point_departure_lambdas[i] = p->point_departure[i];
+        prediction_cores[i] = p->cores[i];
+    }
+    if (p->train) CUSCAN_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CUSCAN_OK;
+}
+
+namespace {
+// PredictionHierarchy::from_state (prediction.rs:279-433): every column is untrusted.
+int import_state(cuscan_ctx *ctx, cuscan_predictor &P, int64_t nn, const uint64_t *node_ids,
+                 const uint64_t *parents, const double *births, const int32_t *labels,
+                 const double *maxes, const uint64_t *point_nodes, const double *departures) {
+    const int64_t nf = P.n_finite;
+    if (nf > INT32_MAX || nn > INT32_MAX)
+        return fail(ctx, CUSCAN_OVERFLOW, "portable prediction hierarchy count");
+    for (int64_t i = 0; i < nf; ++i)
+        if (P.finite_index[i] > (uint32_t)INT32_MAX ||
+            (i > 0 && P.finite_index[i - 1] >= P.finite_index[i]))
+            return invalid(ctx, "portable finite index must be strictly ascending and fit i32");
+    std::unordered_map<uint64_t, int64_t> seen;
+    seen.reserve((size_t)nn * 2);
+    uint64_t min_id = UINT64_MAX;
+    for (int64_t i = 0; i < nn; ++i) {
+        if (!seen.emplace(node_ids[i], i).second)
+            return invalid(ctx, "portable hierarchy node ids are not unique");
+        min_id = node_ids[i] < min_id ? node_ids[i] : min_id;
+    }
+    if (node_ids[0] != min_id)
+        return invalid(ctx, "portable hierarchy root is not the minimum node id");
+    uint64_t zero_bits = 0, b0 = 0;
+    std::memcpy(&b0, &births[0], sizeof(b0));
+    if (parents[0] != UINT64_MAX || b0 != zero_bits)
+        return invalid(ctx, "portable hierarchy root sentinel or birth lambda is not canonical");
+    for (int64_t i = 1; i < nn; ++i) {
+        const uint64_t par = parents[i];
+        if (par >= (uint64_t)nn || par == (uint64_t)i || node_ids[par] >= node_ids[i] ||
+            node_ids[i] <= node_ids[0])
+            return invalid(ctx, "portable hierarchy parent graph is invalid");
+    }
+    std::unordered_map<int32_t, int> used;
+    if (labels[0] >= 0) used.emplace(labels[0], 1);
+    for (int64_t i = 0; i < nn; ++i) {
+        if (std::isnan(births[i]) || births[i] < 0.0 || std::isnan(maxes[i]) || maxes[i] < 0.0 ||
+            labels[i] < -1)
+            return invalid(ctx, "portable hierarchy contains an invalid lambda or label");
+        if (i == 0) {
+            uint64_t mb = 0;
+            std::memcpy(&mb, &maxes[0], sizeof(mb));
+            if (labels[0] == -1 && mb != zero_bits)
+                return invalid(ctx, "unmapped portable hierarchy root must have canonical zero "
+                                    "maximum");
+        } else {
+            const int64_t par = (int64_t)parents[i];
+            if (labels[i] == labels[par]) {
+                uint64_t a = 0, b = 0;
+                std::memcpy(&a, &maxes[i], sizeof(a));
+                std::memcpy(&b, &maxes[par], sizeof(b));
+                if (a != b)
+                    return invalid(ctx, "inherited portable hierarchy maximum differs from its "
+                                        "parent");
+            } else if (labels[i] < 0 || !used.emplace(labels[i], 1).second) {
+                return invalid(ctx, "portable hierarchy anchor labels are invalid or duplicated");
+            }
+        }
+    }
+    for (int64_t i = 0; i < nf; ++i)
+        if (point_nodes[i] >= (uint64_t)nn || std::isnan(departures[i]) || departures[i] < 0.0)
+            return invalid(ctx, "portable point attachment is invalid");
+    P.node_id.resize((size_t)nn);
+    P.node_parent.resize((size_t)nn);
+    P.node_birth.assign(births, births + nn);
+    P.node_label.assign(labels, labels + nn);
+    P.node_max.assign(maxes, maxes + nn);
+    for (int64_t i = 0; i < nn; ++i) {
+        P.node_id[i] = (int64_t)node_ids[i];
+        P.node_parent[i] = i == 0 ? -1 : (int64_t)parents[i];
+    }
+    P.point_node.resize((size_t)nf);
+    for (int64_t i = 0; i < nf; ++i) P.point_node[i] = (int64_t)point_nodes[i];
+    P.point_departure.assign(departures, departures + nf);
+    return CUSCAN_OK;
+}
+}  // namespace
+
+int cuscan_predictor_from_state(cuscan_ctx *ctx, const float *geometry, int64_t n_finite,
+                                int32_t d, int32_t min_samples, const uint32_t *finite_index,
+                                int64_t cluster_nodes, const uint64_t *node_ids,
+                                const uint64_t *node_parent_indices,
+                                const double *node_birth_lambdas, const int32_t *node_labels,
+                                const double *node_max_lambdas,
+                                const uint64_t *point_node_indices,
+                                const double *point_departure_lambdas,
+                                const double *prediction_cores, cuscan_predictor **out,
+                                char *err, size_t err_len) {
+    if (!out) return CUSCAN_INVALID_INPUT;
+    *out = nullptr;
+    cuscan_ctx local;
+    cuscan_ctx *ectx = ctx ? ctx : &local;
+    clear_error(ectx);
+    auto finish = [&](int rc) {
+        if (rc && err && err_len) std::snprintf(err, err_len, "%s", ectx->err);
+        return rc;
+    };
+    if (d <= 0 || min_samples <= 0)
+        return finish(fail(ectx, CUSCAN_INVALID_INPUT,
+                           "predictor feature count and min_samples must be positive"));
+    auto P = std::make_unique<cuscan_predictor>();
+    P->d = d;
+    P->s = min_samples;
+    if (n_finite == 0 && cluster_nodes == 0) {  // the no-cluster-tree state
+        *out = P.release();
+        return CUSCAN_OK;
+    }
+    if (n_finite <= 0 || cluster_nodes <= 0)
+        return finish(invalid(ectx, "portable prediction hierarchy has a partially empty column set"));
+    if (!finite_index || !node_ids || !node_parent_indices || !node_birth_lambdas ||
+        !node_labels || !node_max_lambdas || !point_node_indices || !point_departure_lambdas ||
+        !prediction_cores)
+        return finish(fail(ectx, CUSCAN_INVALID_INPUT, "predictor state received a null pointer"));
+    if (2 * (int64_t)min_samples > n_finite)
+        return finish(invalid(ectx, "predictor min_samples exceeds candidate-width limit"));
+    if (geometry && !ctx)
+        return finish(fail(ectx, CUSCAN_INVALID_INPUT, "predictor geometry needs a device context"));
+    P->n_finite = n_finite;
+    P->finite_index.assign(finite_index, finite_index + n_finite);
+    int rc = import_state(ectx, *P, cluster_nodes, node_ids, node_parent_indices,
+                          node_birth_lambdas, node_labels, node_max_lambdas, point_node_indices,
+                          point_departure_lambdas);
+    if (rc) return finish(rc);
+    P->cores.assign(prediction_cores, prediction_cores + n_finite);
+    // import_predictor_state (crates/hdbscan/src/prediction.rs:1411-1424).
+    for (double c : P->cores) {
+        if (!std::isfinite(c) || c < 0.0)
+            return finish(invalid(ectx, "prediction cores must be finite, nonnegative, and match "
+                                        "finite rows"));
+        uint64_t bits = 0;
+        std::memcpy(&bits, &c, sizeof(bits));
+        if (min_samples == 1 && bits != 0)
+            return finish(invalid(ectx, "rank-one prediction cores must be canonical positive zero"));
+    }
+    if (!geometry) {  // host-only: the candidate math without device searches
+        *out = P.release();
+        return CUSCAN_OK;
+    }
+    for (int64_t i = 0; i < n_finite * (int64_t)d; ++i)
+        if (!std::isfinite(geometry[i]))
+            return finish(invalid(ectx, "predictor geometry must be finite"));
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = sizeof(float) * (size_t)n_finite * d;
+    cudaError_t e = cudaMalloc(&P->train, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return finish(fail(ctx, CUSCAN_MEMORY, "device allocation of %zu bytes for the training "
+                           "rows failed", bytes));
+    }
+    P->device = ctx->device;
+    e = cudaMemcpyAsync(P->train, geometry, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(P->train);
+        P->train = nullptr;
+        return finish(cuda_fail(ctx, e, "predictor geometry upload"));
+    }
+    *out = P.release();
+    return CUSCAN_OK;
+}
+
 int cuscan_predictor_shape(const cuscan_predictor *p, int64_t *n_finite, int32_t *d,
                            int32_t *min_samples) {
     if (!p) return CUSCAN_INVALID_INPUT;

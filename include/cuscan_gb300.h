@@ -266,6 +266,35 @@ int cuscan_predictor_create(cuscan_ctx *ctx, const float *train, int64_t n_finit
 void cuscan_predictor_destroy(cuscan_predictor *p);
 int cuscan_predictor_shape(const cuscan_predictor *p, int64_t *n_finite, int32_t *d,
                            int32_t *min_samples);
+/*
+ * Portable predictor state: the columns of the reference's PredictionHierarchyState
+ * (crates/hdbscan-core/src/prediction.rs:161-272) plus the geometry and the prediction cores,
+ * the arrays of its HDF5 predictor schema v1 (python/cuscan/_hdbscan_predictor_serialization_v1.py).
+ * The no-cluster-tree state has n_finite = cluster_nodes = 0 and no arrays. Node 0 is the root,
+ * its parent index UINT64_MAX. cuscan_predictor_from_state validates every column as
+ * PredictionHierarchy::from_state does (prediction.rs:279-433) and copies the geometry
+ * ([n_finite * d] f32) to the context's device. A host-only predictor (created without training
+ * rows) exports with ctx and geometry NULL, and from_state with geometry NULL (ctx may be NULL)
+ * builds one: it runs cuscan_predictor_predict_candidates but not cuscan_predictor_predict.
+ */
+int cuscan_predictor_state_shape(const cuscan_predictor *p, int64_t *n_finite,
+                                 int64_t *cluster_nodes);
+int cuscan_predictor_export(cuscan_ctx *ctx, const cuscan_predictor *p, float *geometry,
+                            uint32_t *finite_index, uint64_t *node_ids,
+                            uint64_t *node_parent_indices, double *node_birth_lambdas,
+                            int32_t *node_labels, double *node_max_lambdas,
+                            uint64_t *point_node_indices, double *point_departure_lambdas,
+                            double *prediction_cores);
+int cuscan_predictor_from_state(cuscan_ctx *ctx, const float *geometry, int64_t n_finite,
+                                int32_t d, int32_t min_samples, const uint32_t *finite_index,
+                                int64_t cluster_nodes, const uint64_t *node_ids,
+                                const uint64_t *node_parent_indices,
+                                const double *node_birth_lambdas, const int32_t *node_labels,
+                                const double *node_max_lambdas,
+                                const uint64_t *point_node_indices,
+                                const double *point_departure_lambdas,
+                                const double *prediction_cores, cuscan_predictor **out,
+                                char *err, size_t err_len);
 /* Upper bound on the context workspace one cuscan_predictor_predict of m rows allocates. */
 int64_t cuscan_predict_workspace_bytes(const cuscan_predictor *p, int64_t m);
 /* 1 when the fitted tree has no clusters (every prediction is noise, 0, -1). */
