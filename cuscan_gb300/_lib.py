@@ -111,6 +111,7 @@ class FitStats(C.Structure):
         ("cross_pairs", C.c_double),
         ("rescreened_rows", C.c_int64),
         ("screen_tile_pairs", C.c_int64),
+        ("boruvka_screened_rows", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

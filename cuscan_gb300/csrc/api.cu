@@ -260,6 +260,8 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     b.refined.want_fp16 = precision == CUSCAN_PRECISION_FP16_REFINED;
     b.refined.have_scale = false;
     b.refined.tile_pairs = 0;
+    b.refined.screened_rows = 0;
+    b.refined.lb_valid = false;
 
     CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
@@ -330,6 +332,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->cross_pairs = cross_pairs;
         stats->rescreened_rows = rescreened_rows;
         stats->screen_tile_pairs = b.refined.tile_pairs;
+        stats->boruvka_screened_rows = b.refined.screened_rows;
     }
     return CUSCAN_OK;
 }

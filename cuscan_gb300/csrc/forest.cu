@@ -526,7 +526,8 @@ int forest_buffers(ForestBuffers &b, Buffer **out) {
                      &r.tile_hi, &r.cand_ids, &r.cand_lb, &r.fallback, &r.count, &r.error,
                      &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d, &r.absmax,
                      &r.qthr, &r.xq, &r.pq, &r.mq, &r.cand2, &r.rowcnt2, &r.fallback2,
-                     &r.urow, &r.colcnt, &r.colbuf};
+                     &r.urow, &r.colcnt, &r.colbuf, &r.act_flag, &r.act_idx, &r.act_pos,
+                     &r.rowlb, &r.lbtmp};
     static_assert(sizeof(all) / sizeof(all[0]) == kForestBufferCount, "buffer list");
     const int count = (int)(sizeof(all) / sizeof(all[0]));
     if (out)

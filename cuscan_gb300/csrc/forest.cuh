@@ -20,12 +20,16 @@ struct RefinedBuffers {
     Buffer error, cbound, rowcnt, pivots, cells, cell_d, absmax;
     Buffer qthr, xq, pq, mq, cand2, rowcnt2, fallback2;  // threshold re-screen of kNN rows
     Buffer urow, colcnt, colbuf;  // symmetric Borůvka: row bounds, column-side buffers
+    Buffer act_flag, act_idx, act_pos;  // Borůvka rows that can hold their component's edge
+    Buffer rowlb, lbtmp;  // lower bounds of each row's cheapest cross edge (original order)
     // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
     bool want_fp16 = false;  // requested by the caller's precision
     bool fp16 = false;       // in use (the data's range allows a scale)
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;
     int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
+    int64_t screened_rows = 0;  // query rows of the current fit's Borůvka screens
+    bool lb_valid = false;      // rowlb holds bounds of the current fit
 };
 
 struct ForestBuffers {
@@ -45,7 +49,7 @@ struct ForestBuffers {
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
 void forest_release(ForestBuffers &b);
 // Every device buffer of the forest and of the bf16 screen (out may be null); returns the count.
-constexpr int kForestBufferCount = 55;
+constexpr int kForestBufferCount = 60;
 int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);

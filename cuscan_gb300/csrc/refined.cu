@@ -81,6 +81,9 @@ struct Params {
     int32_t *colcnt;
     int32_t *colbuf;
     int capc;
+    // one-sided Borůvka: per query row and column half, a lower bound of every cross-component
+    // pair weight the row has (raw f32, rounded down)
+    float *rowlb;
 };
 
 // Screen modes: kNN lists, Borůvka thresholds with shared component bounds, kNN thresholds.
@@ -94,6 +97,7 @@ constexpr int MODE_BORUVKA_SYM = 3;
 constexpr int BORUVKA_COL_CAP = 64;  // column-side candidate slots per row
 constexpr double SYM_UNBOUNDED_MAX = 0.25;  // largest share of unbounded rows for the symmetric screen
 constexpr int64_t SYM_MIN_ROWS = 131072;     // smallest point set for the symmetric screen
+constexpr double SYM_ACTIVE_MIN = 0.9;  // smallest share of screened rows for the symmetric screen
 constexpr int KNN_CAP = 512;  // threshold-mode candidate slots per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
@@ -380,6 +384,11 @@ __device__ __forceinline__ int64_t block_at(const Params &P, int64_t qi) {
 // Label range of query block qb (4 chunks of 32 rows).
 __device__ __forceinline__ void qblock_range(const Params &P, int64_t qb, int32_t &lo,
                                              int32_t &hi) {
+    if (P.qpos) {  // gathered query rows: no label range (no tile is skipped)
+        lo = INT32_MIN;
+        hi = INT32_MAX;
+        return;
+    }
     lo = INT32_MAX;
     hi = INT32_MIN;
     for (int64_t c = qb * 4; c < qb * 4 + 4 && c < P.n_chunks; ++c) {
@@ -597,8 +606,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             float core_i = 0.0f;
             int32_t lab_i = -1;
             if (BORUVKA && valid) {
-                core_i = P.core[row] * P.s2;
-                lab_i = P.label[row];
+                core_i = P.core[self] * P.s2;
+                lab_i = P.label[self];
             }
             // kNN threshold mode: a fixed upper bound of the row's k-th distance (scaled); a row
             // without one overflows its buffer at once and is resolved exactly
@@ -617,6 +626,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 J[s2] = -1;
             }
             float U = CUSCAN_INF, published = CUSCAN_INF;
+            float lb_all = CUSCAN_INF;  // one-sided Borůvka: min chunk bound over cross chunks
             int cnt = 0;
             int32_t qlo = 0, qhi = 0;
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
@@ -783,19 +793,33 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 // fmaf(-2, max v, min pb) is below (or equal to) every element's
                 // fmaf(-2, v_j, pb_j) and min core + dlt bounds the core term, because rounding
                 // is monotonic.
-                unsigned hitbits = 0;
+                unsigned hitbits = 0, mixbits = 0;
                 {
                     const bool row_on = valid && tau_ok && (!BORUVKA || core_i <= T);
 #pragma unroll
                     for (int c = 0; c < HALF / 32; ++c) {
-                        bool on = row_on;
+                        int32_t clo = 0, chi = 0;
                         if (BORUVKA) {
-                            const int32_t clo = __shfl_sync(0xffffffffu, ch_word, c);
-                            const int32_t chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
-                            if (clo == -2 || (clo == lab_i && chi == lab_i)) on = false;
+                            clo = __shfl_sync(0xffffffffu, ch_word, c);
+                            chi = __shfl_sync(0xffffffffu, ch_word, 4 + c);
                         }
+                        const bool cross = !BORUVKA || (clo != -2 && !(clo == lab_i && chi == lab_i));
+                        const bool on = row_on && cross;
                         const float2 cmin = chunk_min[c];
                         float flb = fmaf(-2.0f, vmax[c], cmin.x);
+                        if (MODE == MODE_BORUVKA && cross) {
+                            if (clo <= lab_i && lab_i <= chi) {
+                                // the chunk also holds rows of the row's own component: its
+                                // bound may come from those, so it is taken pair by pair below
+                                mixbits |= 1u << c;
+                            } else {
+                                // below every pair of the chunk: mb <= mt, dot <= vmax,
+                                // pb >= min pb, core_j >= min core, and fmaf/add rounding is
+                                // monotonic
+                                const float lbc = fmaf(-cm_i, mt, flb + ps_i);
+                                lb_all = fminf(lb_all, fmaxf(fmaxf(lbc, core_i), cmin.y));
+                            }
+                        }
                         if (BORUVKA) flb = fmaxf(flb, cmin.y + dlt);
                         if (on && flb < thr_fast) hitbits |= 1u << c;
                     }
@@ -953,6 +977,29 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         thresholds();
                     }
                 }
+                // one-sided Borůvka: row bounds over the chunks shared with the own component,
+                // other components' pairs only (at most a couple of chunks per component)
+                if (MODE == MODE_BORUVKA) {
+                    const unsigned wmix = __reduce_or_sync(0xffffffffu, mixbits);
+                    for (int c = 0; wmix != 0 && c < HALF / 32; ++c) {
+                        if (!((wmix >> c) & 1u)) continue;
+                        uint32_t rm[32];
+                        tmem_ld32_issue(taddr + c * 32, rm);
+                        tmem_ld_wait(rm);
+                        if ((mixbits >> c) & 1u) {
+                            const int64_t j0 = t * BN + half * HALF + c * 32;
+#pragma unroll 4
+                            for (int e = 0; e < 32; ++e) {
+                                const int col = c * 32 + e;
+                                if (j0 + e >= P.n || P.label[j0 + e] == lab_i) continue;
+                                const float lb = fmaf(-cm_i, mb[col],
+                                                      fmaf(-2.0f, __uint_as_float(rm[e]), pb[col]) + ps_i);
+                                lb_all = fminf(lb_all, fmaxf(fmaxf(lb, core_i), cb[col]));
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
                 fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&t_empty[b]);
@@ -970,6 +1017,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             if (APPEND) {
                 // each half of a row appends into its own slot range [(2 row + half) * cap, +cap)
                 if (valid) P.rowcnt[row * 2 + half] = tau_ok ? cnt : P.cap + 1;
+                if (MODE == MODE_BORUVKA && valid && P.rowlb)
+                    P.rowlb[row * 2 + half] = __fmul_rd(lb_all, P.inv_s2);
             } else if (valid) {
                 const int64_t base_at = row * (2 * M) + half * M;
 #pragma unroll
@@ -1183,7 +1232,8 @@ __global__ void positions_to_rows_kernel(int32_t *__restrict__ list, int64_t cou
 // their component's cheapest edge: every pair reaching it is appended).
 __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float *__restrict__ corep,
                                       const int32_t *__restrict__ labp,
-                                      const int32_t *__restrict__ perm, int64_t n, int d,
+                                      const int32_t *__restrict__ perm, int64_t nq,
+                                      const int32_t *__restrict__ qpos, int d,
                                       const int32_t *__restrict__ cand_ids,
                                       const int32_t *__restrict__ rowcnt, int cap,
                                       const int32_t *__restrict__ colcnt,
@@ -1191,10 +1241,12 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
                                       unsigned long long *__restrict__ row_keys,
                                       int32_t *__restrict__ fallback,
                                       int *__restrict__ fallback_count) {
-    const int64_t pos = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    // q indexes the screened rows (all positions, or the gathered positions qpos)
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (pos >= n) return;
-    const int c0 = rowcnt[pos * 2], c1 = rowcnt[pos * 2 + 1];
+    if (q >= nq) return;
+    const int64_t pos = qpos ? (int64_t)qpos[q] : q;
+    const int c0 = rowcnt[q * 2], c1 = rowcnt[q * 2 + 1];
     const int c2 = colcnt ? colcnt[pos] : 0;  // pairs other blocks appended for this row
     if (c0 > cap || c1 > cap || c2 > capc) {
         if (lane == 0) {
@@ -1217,8 +1269,8 @@ __global__ void rerank_boruvka_kernel(const float *__restrict__ xp, const float 
         const int s = base + lane;
         int32_t j = -1;
         if (s < total) {
-            j = s < c0        ? cand_ids[(pos * 2) * cap + s]
-                : s < c0 + c1 ? cand_ids[(pos * 2 + 1) * cap + (s - c0)]
+            j = s < c0        ? cand_ids[(q * 2) * cap + s]
+                : s < c0 + c1 ? cand_ids[(q * 2 + 1) * cap + (s - c0)]
                               : colbuf[pos * capc + (s - c0 - c1)];
             if (labp[j] == li) j = -1;
         }
@@ -1266,18 +1318,50 @@ __global__ void pick_pivots_kernel(const float *__restrict__ x, int64_t n, int d
 
 // Per-row bounds of the symmetric screen: the bound of the row's component.
 // Also counts the rows whose component has no bound yet.
+// Row bounds of the symmetric screen (the component bounds), the count of rows without one, and
+// the rows that can hold their component's cheapest edge. Every edge of row i weighs at least
+// core_i and at least the row's lower bound from earlier rounds (its component has only grown
+// since, so it has fewer cross edges); a row where either exceeds its component's upper bound
+// cannot hold the cheapest edge, ties included.
 __global__ void init_row_bounds_kernel(const uint32_t *__restrict__ cbound,
-                                       const int32_t *__restrict__ labp, int64_t n,
-                                       uint32_t *__restrict__ urow, int *__restrict__ unbounded) {
+                                       const int32_t *__restrict__ labp,
+                                       const float *__restrict__ corep,
+                                       const float *__restrict__ rowlb,
+                                       const int32_t *__restrict__ perm, int64_t n,
+                                       uint32_t *__restrict__ urow, int *__restrict__ unbounded,
+                                       int32_t *__restrict__ active) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool inf = false;
     if (i < n) {
         const uint32_t b = cbound[labp[i]];
         urow[i] = b;
         inf = b >= 0x7f800000u;
+        const float ub = __uint_as_float(b);
+        active[i] = !(corep[i] > ub) && !(rowlb[perm[i]] > ub) ? 1 : 0;
     }
     const unsigned m = __ballot_sync(0xffffffffu, inf);
     if ((threadIdx.x & 31) == 0 && m) atomicAdd(unbounded, __popc(m));
+}
+
+// Fold the one-sided screen's bounds (two column halves per query row) into the per-row lower
+// bounds, kept in original row order across rounds.
+__global__ void update_row_lb_kernel(const float *__restrict__ lbtmp,
+                                     const int32_t *__restrict__ qpos,
+                                     const int32_t *__restrict__ perm, int64_t nq,
+                                     float *__restrict__ rowlb) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int64_t pos = qpos ? (int64_t)qpos[q] : q;
+    const int32_t orow = perm[pos];
+    rowlb[orow] = fmaxf(rowlb[orow], fminf(lbtmp[2 * q], lbtmp[2 * q + 1]));
+}
+
+// Positions of the flagged rows, in order (idx is the exclusive scan of the flags).
+__global__ void compact_positions_kernel(const int32_t *__restrict__ flag,
+                                         const int32_t *__restrict__ idx, int64_t n,
+                                         int32_t *__restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) out[idx[i]] = (int32_t)i;
 }
 
 __global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
@@ -1370,8 +1454,10 @@ size_t refined_workspace_bytes(int64_t n, int d, int k) {
     // candidates, counts, fallback list
     b += 4 * (size_t)n + (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;
     b += 4 * (size_t)n * 2 * KNN_CAP + 8 * (size_t)n + 4 * (size_t)n;
-    // symmetric Borůvka: row bounds, column-side counts and candidates
-    b += 8 * (size_t)n + 4 * (size_t)n * BORUVKA_COL_CAP;
+    // symmetric Borůvka: row bounds, column-side counts and candidates; subset rounds: flags,
+    // their scan and the gathered positions
+    b += 8 * (size_t)n + 4 * (size_t)n * BORUVKA_COL_CAP + 12 * (size_t)n;
+    b += 12 * (size_t)n;  // row lower bounds (original order) and per-half screen bounds
     return b;
 }
 
@@ -1457,6 +1543,7 @@ struct QuerySet {
     const float *qthr = nullptr;
     int32_t *cand_ids = nullptr;
     int32_t *rowcnt = nullptr;
+    float *rowlb = nullptr;  // one-sided Borůvka: per query row and half, the pair lower bound
 };
 
 template <int M, int MODE>
@@ -1520,6 +1607,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         P.colbuf = as<int32_t>(R.colbuf);
         P.capc = BORUVKA_COL_CAP;
     }
+    if (MODE == MODE_BORUVKA) P.rowlb = Q.rowlb;
     if (MODE == MODE_KNN_THRESHOLD) {
         P.cap = KNN_CAP;
         P.cand_ids = Q.cand_ids;
@@ -1679,38 +1767,94 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     if ((rc = ensure(ctx, R.colcnt, sizeof(int32_t) * n, "column-side counts"))) return rc;
     if ((rc = ensure(ctx, R.colbuf, sizeof(int32_t) * n * BORUVKA_COL_CAP, "column-side candidates")))
         return rc;
-    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.colcnt.ptr, 0, sizeof(int32_t) * n, s));
-    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    CUSCAN_KERNEL(init_row_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
-                  as<uint32_t>(R.cbound), labp, n, as<uint32_t>(R.urow), as<int>(R.count));
-    CUSCAN_LAUNCH(ctx, "init_row_bounds_kernel");
-    // The symmetric screen halves the tensor-core and epilogue work but tests a pair for its
-    // column's row only against that row's known bound; rows of components without a bound
-    // draw many appends there. Small sets (where fixed costs dominate) and rounds with many
-    // unbounded rows run the one-sided screen.
-    bool sym = n >= SYM_MIN_ROWS;
-    if (sym) {
-        int unbounded = 0;
-        CUSCAN_CUDA(ctx, cudaMemcpyAsync(&unbounded, R.count.ptr, sizeof(int),
-                                         cudaMemcpyDeviceToHost, s));
-        CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
-        sym = (double)unbounded <= SYM_UNBOUNDED_MAX * (double)n;
+    rc = ensure(ctx, R.act_flag, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.act_idx, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.act_pos, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.rowlb, sizeof(float) * n, "row lower bounds");
+    if (!rc) rc = ensure(ctx, R.lbtmp, sizeof(float) * 2 * n, "row lower bounds");
+    if (rc) return rc;
+    if (!R.lb_valid) {  // first round of the fit: no bounds yet
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowlb.ptr, 0, sizeof(float) * n, s));
+        R.lb_valid = true;
     }
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.colcnt.ptr, 0, sizeof(int32_t) * n, s));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, 2 * sizeof(int), s));
+    CUSCAN_KERNEL(init_row_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
+                  as<uint32_t>(R.cbound), labp, corep, as<float>(R.rowlb), perm, n,
+                  as<uint32_t>(R.urow), as<int>(R.count), as<int32_t>(R.act_flag));
+    CUSCAN_LAUNCH(ctx, "init_row_bounds_kernel");
+    if ((rc = scan_exclusive(ctx, as<int32_t>(R.act_flag), as<int32_t>(R.act_idx), n,
+                             as<int32_t>(R.count) + 1, b.scan_tmp, s)))
+        return rc;
+    int counts[2] = {0, 0};  // rows without a component bound, rows that can hold an edge
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(counts, R.count.ptr, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    const int64_t active = counts[1];
+    // Forms of the round:
+    //  * one-sided over the rows that can hold their component's cheapest edge (all rows, or a
+    //    gathered subset): it also leaves each screened row a lower bound of its cheapest cross
+    //    edge, which lets most rows skip the later rounds. After the kNN seed most components
+    //    have a bound from a neighbour in another component and few rows are that close to the
+    //    boundary; later rounds skip the rows whose earlier bound already exceeds the bound.
+    //  * symmetric: each unordered pair once. It halves the tensor-core and epilogue work but
+    //    leaves no row bounds and tests a pair for its column's row only against that row's
+    //    known bound (rows of components without a bound draw many appends there); it is used
+    //    only when nearly every row is screened.
+    const bool sym = n >= SYM_MIN_ROWS &&
+                     (double)counts[0] <= SYM_UNBOUNDED_MAX * (double)n &&
+                     (double)active > SYM_ACTIVE_MIN * (double)n;
+    const bool subset = !sym && active < n;
     CUSCAN_LAUNCH(ctx, "component bounds");
     constexpr int M = 32;
-    if (sym) rc = run_screen<M, MODE_BORUVKA_SYM>(ctx, R, L, n, d, corep, labp, clo, chi, s);
-    else rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s);
+    const int32_t *qpos = nullptr;
+    int64_t nq = n;
+    if (subset) {
+        nq = active;
+        const int64_t nq_pad = ceil_div(nq > 0 ? nq : 1, (int64_t)BN) * BN;
+        rc = ensure(ctx, R.xq, (size_t)nq_pad * L.d_pad * 2, "subset tiles");
+        if (!rc) rc = ensure(ctx, R.pq, sizeof(float) * nq_pad, "subset norms");
+        if (!rc) rc = ensure(ctx, R.mq, sizeof(float) * nq_pad, "subset norms");
+        if (rc) return rc;
+        CUSCAN_KERNEL(compact_positions_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
+                      as<int32_t>(R.act_flag), as<int32_t>(R.act_idx), n, as<int32_t>(R.act_pos));
+        CUSCAN_LAUNCH(ctx, "compact_positions_kernel");
+        qpos = as<int32_t>(R.act_pos);
+        if ((rc = tile_rows(ctx, R, xp, nq, d, L.d_pad, nq_pad, qpos, as<uint8_t>(R.xq),
+                            as<float>(R.pq), as<float>(R.mq), s)))
+            return rc;
+        QuerySet Q;
+        Q.xq = as<uint8_t>(R.xq);
+        Q.pq = as<float>(R.pq);
+        Q.mq = as<float>(R.mq);
+        Q.nq = nq;
+        Q.qpos = qpos;
+        Q.rowlb = as<float>(R.lbtmp);
+        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, Q);
+    } else if (sym) {
+        rc = run_screen<M, MODE_BORUVKA_SYM>(ctx, R, L, n, d, corep, labp, clo, chi, s);
+    } else {
+        QuerySet Q;
+        Q.rowlb = as<float>(R.lbtmp);
+        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, Q);
+    }
     if (rc) return rc;
+    if (!sym && nq > 0) {
+        CUSCAN_KERNEL(update_row_lb_kernel, (unsigned)ceil_div(nq, 256), 256, 0, s,
+                      as<float>(R.lbtmp), qpos, perm, nq, as<float>(R.rowlb));
+        CUSCAN_LAUNCH(ctx, "update_row_lb_kernel");
+    }
+    R.screened_rows += nq;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
     if ((rc = allow_dynamic_smem(ctx, rerank_boruvka_kernel, rr_smem))) return rc;
-    CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
-                  32 * RERANK_WARPS, rr_smem, s, xp, corep,
-                  labp, perm, n, d, as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
-                  sym ? as<int32_t>(R.colcnt) : nullptr, as<int32_t>(R.colbuf), BORUVKA_COL_CAP,
-                  row_keys,
-                  as<int32_t>(R.fallback), as<int>(R.count));
-    CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
+    if (nq > 0) {
+        CUSCAN_KERNEL(rerank_boruvka_kernel, (unsigned)ceil_div(nq, (int64_t)RERANK_WARPS),
+                      32 * RERANK_WARPS, rr_smem, s, xp, corep, labp, perm, nq, qpos, d,
+                      as<int32_t>(R.cand_ids), as<int32_t>(R.rowcnt), BORUVKA_CAP,
+                      sym ? as<int32_t>(R.colcnt) : nullptr, as<int32_t>(R.colbuf),
+                      BORUVKA_COL_CAP, row_keys, as<int32_t>(R.fallback), as<int>(R.count));
+        CUSCAN_LAUNCH(ctx, "rerank_boruvka_kernel");
+    }
     int fallbacks = 0;
     if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
     if (fallback_rows) *fallback_rows += fallbacks;

@@ -84,6 +84,8 @@ typedef struct cuscan_fit_stats {
     double cross_pairs;      /* sum over rounds of ordered cross-component pairs */
     int64_t rescreened_rows; /* kNN rows screened a second time in threshold mode */
     int64_t screen_tile_pairs; /* 128 x 256 tensor-core tiles the screens computed */
+    int64_t boruvka_screened_rows; /* query rows of the Boruvka screens, summed over rounds
+                                      (rows whose core exceeds their component's bound skip) */
 } cuscan_fit_stats;
 
 /* ---- context ---- */
