@@ -99,6 +99,7 @@ constexpr double SYM_UNBOUNDED_MAX = 0.25;  // largest share of unbounded rows f
 constexpr int64_t SYM_MIN_ROWS = 131072;     // smallest point set for the symmetric screen
 constexpr double SYM_ACTIVE_MIN = 0.9;  // smallest share of screened rows for the symmetric screen
 constexpr int KNN_CAP = 512;  // threshold-mode candidate slots per row half
+constexpr int KNN_LIST = 24;  // kNN list entries per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
 // ---- PTX wrappers ----
@@ -744,34 +745,47 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 // released only after this tile) and tested element by element.
                 constexpr bool PIPE = APPEND;
                 float vmax[HALF / 32];
-                {
-                    uint32_t rA[32], rB[PIPE ? 32 : 1];
+                if constexpr (PIPE) {
+                    uint32_t rA[32], rB[32];
                     tmem_ld32_issue(taddr, rA);
                     tmem_ld_wait(rA);
 #pragma unroll
                     for (int c = 0; c < HALF / 32; ++c) {
-                        if constexpr (PIPE) {
-                            if (c > 0) {
+                        if (c > 0) {
 #pragma unroll
-                                for (int e = 0; e < 32; ++e) rA[e] = rB[e];
-                            }
-                            if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
-                        } else if (c > 0) {
-                            tmem_ld32_issue(taddr + c * 32, rA);
-                            tmem_ld_wait(rA);
+                            for (int e = 0; e < 32; ++e) rA[e] = rB[e];
                         }
+                        if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
                         float v[32];
 #pragma unroll
                         for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(rA[e]);
+                        vmax[c] = max32(v);
+                        if (c + 1 < HALF / 32) tmem_ld_wait(rB);
+                    }
+                } else {
+                    // kNN lists: two chunks per wait (the lists leave no room to pipeline)
+#pragma unroll
+                    for (int c = 0; c < HALF / 32; c += 2) {
+                        uint32_t rA[32], rB[32];
+                        tmem_ld32_issue(taddr + c * 32, rA);
+                        tmem_ld32_issue(taddr + (c + 1) * 32, rB);
+                        tmem_ld_wait(rA);
+                        tmem_ld_wait(rB);
+                        float v[32], w[32];
+#pragma unroll
+                        for (int e = 0; e < 32; ++e) {
+                            v[e] = __uint_as_float(rA[e]);
+                            w[e] = __uint_as_float(rB[e]);
+                        }
                         if (debug && tcount == 0) {
 #pragma unroll
-                            for (int e = 0; e < 32; ++e)
+                            for (int e = 0; e < 32; ++e) {
                                 P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
+                                P.debug_tile[row_local * BN + half * HALF + (c + 1) * 32 + e] = w[e];
+                            }
                         }
                         vmax[c] = max32(v);
-                        if constexpr (PIPE) {
-                            if (c + 1 < HALF / 32) tmem_ld_wait(rB);
-                        }
+                        vmax[c + 1] = max32(w);
                     }
                 }
                 // Thresholds moved to the scale of F = (1 - C_B) p_j - 2 dot with the tile's
@@ -1122,12 +1136,12 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__
     for (int f = lane; f < d; f += 32) q_s[f] = x[row * d + f];
     __syncwarp();
     constexpr int W = 2 * M;  // two lists of M per row (one per column half)
-    constexpr int PER = W / 32;
+    constexpr int PER = (W + 31) / 32;
     unsigned long long key[PER];
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const int s = q * 32 + lane;
-        const int32_t j = cand_ids[row * W + s];
+        const int32_t j = s < W ? cand_ids[row * W + s] : -1;
         const float dd = staged_d2(x, d, q_s, j, rows_s, lane);
         key[q] = j < 0 ? ~0ull : ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
     }
@@ -1671,7 +1685,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     const int32_t *perm = as<int32_t>(b.perm);
     // 3. screen + exact re-rank in sorted positions, outputs in original rows
     if ((rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s))) return rc;
-    constexpr int M = 32;
+    // 24 bounds per row half: enough that nearly every row's unseen bound clears its k-th
+    // exact distance at k <= 32 for bf16 screens, and each insertion shifts 24 registers
+    constexpr int M = KNN_LIST;
     if ((rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
