@@ -1072,13 +1072,18 @@ __device__ __forceinline__ float exact_d2(const float *__restrict__ a, const flo
 __device__ __forceinline__ float staged_d2(const float *__restrict__ x, int d,
                                            const float *q_s, int32_t j, float *rows_s,
                                            int lane) {
+    // asynchronous 4-byte copies: every row's loads are in flight at once
     for (int r = 0; r < 32; ++r) {
         const int32_t jr = __shfl_sync(0xffffffffu, j, r);
         if (jr < 0) continue;
         const float *src = x + (int64_t)jr * d;
         float *dst = rows_s + r * (d + 1);
-        for (int f = lane; f < d; f += 32) dst[f] = src[f];
+        for (int f = lane; f < d; f += 32)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst + f)),
+                         "l"(src + f)
+                         : "memory");
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncwarp();
     float acc = CUSCAN_INF;
     if (j >= 0) {
