@@ -112,6 +112,7 @@ class FitStats(C.Structure):
         ("rescreened_rows", C.c_int64),
         ("screen_tile_pairs", C.c_int64),
         ("boruvka_screened_rows", C.c_int64),
+        ("mst_weight", C.c_double),
     ]
 
     def as_dict(self) -> dict:

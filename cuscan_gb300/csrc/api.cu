@@ -313,6 +313,10 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         ++rounds;
         components = (int64_t)hs->components;
     }
+    // total weight of the tree in f64 on the device (finalize_mst's per-edge sqrt, summed)
+    if ((rc = forest_mst_weight(ctx, b, mst_wsq, (int64_t)hs->edges, s))) return rc;
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&hs->mst_weight, &b.status->mst_weight, sizeof(double),
+                                     cudaMemcpyDeviceToHost, s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[3], s));
     CUSCAN_CUDA(ctx, cudaEventSynchronize(ev[3]));
     if ((int64_t)hs->edges != n - 1)
@@ -333,6 +337,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->rescreened_rows = rescreened_rows;
         stats->screen_tile_pairs = b.refined.tile_pairs;
         stats->boruvka_screened_rows = b.refined.screened_rows;
+        stats->mst_weight = hs->mst_weight;
     }
     return CUSCAN_OK;
 }

@@ -481,6 +481,62 @@ int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t component
     return resolve_proposals(ctx, b, n, components, label, label, out_src, out_dst, out_w, 1, s);
 }
 
+// Total MST weight in f64: the sum over the emitted edges of sqrt((double) w_sq), the per-edge
+// weight that finalize_mst forms (crates/hdbscan-core/src/mst.rs:501-512). Every edge's f64
+// weight is exact (IEEE square root of an exactly widened f32); only the order of the sum is
+// this kernel's own: a fixed grid-stride assignment and a fixed shared-memory tree per block,
+// then one block sums the partials the same way. The result depends only on the edge list.
+constexpr int kWeightThreads = 256;
+constexpr int kWeightBlocks = 256;
+
+__device__ double block_tree_sum(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+#pragma unroll
+    for (int off = kWeightThreads / 2; off > 0; off >>= 1) {
+        if ((int)threadIdx.x < off) sh[threadIdx.x] += sh[threadIdx.x + off];
+        __syncthreads();
+    }
+    return sh[0];
+}
+
+__global__ void __launch_bounds__(kWeightThreads)
+mst_weight_partials_kernel(const float *__restrict__ w, int64_t m, int grid,
+                           double *__restrict__ partials) {
+    __shared__ double sh[kWeightThreads];
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * kWeightThreads + threadIdx.x; i < m;
+         i += (int64_t)grid * kWeightThreads)
+        acc += sqrt((double)w[i]);
+    const double total = block_tree_sum(acc, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kWeightThreads)
+mst_weight_final_kernel(const double *__restrict__ partials, int grid, DevStatus *status) {
+    __shared__ double sh[kWeightThreads];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < grid; i += kWeightThreads) acc += partials[i];
+    const double total = block_tree_sum(acc, sh);
+    if (threadIdx.x == 0) status->mst_weight = total;
+}
+
+int forest_mst_weight(cuscan_ctx *ctx, ForestBuffers &b, const float *w, int64_t m,
+                      cudaStream_t s) {
+    if (m <= 0) {
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(&b.status->mst_weight, 0, sizeof(double), s));
+        return CUSCAN_OK;
+    }
+    // partials live in the component-key array (n 64-bit slots, idle once the rounds end);
+    // the grid never exceeds the edge count, which is below n
+    const int grid = (int)std::min<int64_t>(kWeightBlocks, ceil_div(m, kWeightThreads));
+    double *partials = as<double>(b.comp_keys);
+    CUSCAN_KERNEL(mst_weight_partials_kernel, grid, kWeightThreads, 0, s, w, m, grid, partials);
+    CUSCAN_KERNEL(mst_weight_final_kernel, 1, kWeightThreads, 0, s, partials, grid, b.status);
+    CUSCAN_LAUNCH(ctx, "MST weight");
+    return CUSCAN_OK;
+}
+
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d) {
     const size_t ni = sizeof(int32_t) * (size_t)n;
     int rc = 0;

@@ -12,6 +12,7 @@ struct DevStatus {
     double same_pairs;     // sum of squared component sizes entering the current round
     int err_kind;          // 0 ok, 1 numerical weight, 2 index out of range, 4 no progress
     int pad[3];
+    double mst_weight;     // f64 total MST weight, written once after the last round
 };
 
 // Buffers of the bf16 screening path (refined.cu).
@@ -67,6 +68,10 @@ int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, 
 int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t components,
                  int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
                  cudaStream_t s, int allow_empty = 0);
+// status->mst_weight = sum over the first m edges of sqrt((double) w[i]), reduced in f64 in a
+// fixed order (deterministic for a given edge list).
+int forest_mst_weight(cuscan_ctx *ctx, ForestBuffers &b, const float *w, int64_t m,
+                      cudaStream_t s);
 int scan_exclusive(cuscan_ctx *ctx, const int32_t *in, int32_t *out, int64_t n,
                    int32_t *grand_total, Buffer &tmp, cudaStream_t s);
 

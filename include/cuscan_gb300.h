@@ -86,6 +86,9 @@ typedef struct cuscan_fit_stats {
     int64_t screen_tile_pairs; /* 128 x 256 tensor-core tiles the screens computed */
     int64_t boruvka_screened_rows; /* query rows of the Boruvka screens, summed over rounds
                                       (rows whose core exceeds their component's bound skip) */
+    double mst_weight;       /* total MST weight: sum of sqrt((double) w_sq) over the edges, the
+                                weights finalize_mst forms (mst.rs:501-512), reduced in f64 on
+                                the device in a fixed order */
 } cuscan_fit_stats;
 
 /* ---- context ---- */

@@ -58,6 +58,10 @@ def test_core_and_mst_weight_error_vs_fp64(gpu_ctx, name, n, capsys):
     core32 = out["core_sq"].astype(np.float64)
     rel_core = np.max(np.abs(np.sqrt(core32) - np.sqrt(core64)) / np.sqrt(core64))
     w32 = float(np.sqrt(out["wsq"].astype(np.float64)).sum())
+    # the device's f64 reduction of the same edge weights differs from this host sum only in
+    # the order of the additions
+    w_dev = out["stats"]["mst_weight"]
+    assert abs(w_dev - w32) <= 1e-12 * w32
     w64 = f64_mst_weight(x, core64)
     rel_w = abs(w32 - w64) / w64
     with capsys.disabled():

@@ -23,6 +23,34 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
+def tree_sum(v: np.ndarray) -> np.ndarray:
+    """Shared-memory tree of 256 lanes (lane t adds lane t + off for off = 128, 64, ..., 1)."""
+    v = v.copy()
+    off = v.shape[-1] // 2
+    while off:
+        v[..., :off] = v[..., :off] + v[..., off:2 * off]
+        off //= 2
+    return v[..., 0]
+
+
+def device_order_weight(wsq: np.ndarray) -> float:
+    """The f64 total MST weight summed in the device reduction's order: sqrt((double) w_sq)
+    per edge, grid-stride accumulation over at most 256 blocks of 256 threads, a tree per
+    block, then one tree over the partials."""
+    w = np.sqrt(np.asarray(wsq, np.float32).astype(np.float64))
+    m, lanes = w.size, 256
+    grid = min(256, -(-m // lanes))
+    stride = grid * lanes
+    padded = np.zeros(-(-m // stride) * stride)
+    padded[:m] = w
+    acc = np.zeros((grid, lanes))
+    for j in range(padded.size // stride):
+        acc = acc + padded[j * stride:(j + 1) * stride].reshape(grid, lanes)
+    partial = np.zeros(lanes)
+    partial[:grid] = tree_sum(acc)
+    return float(tree_sum(partial))
+
+
 def assert_fit_equal(got, exp):
     np.testing.assert_array_equal(got["knn_ids"], exp.knn_ids)
     np.testing.assert_array_equal(bits(got["knn_sq"]), bits(exp.knn_sq))
@@ -32,6 +60,7 @@ def assert_fit_equal(got, exp):
     np.testing.assert_array_equal(bits(got["wsq"]), bits(exp.wsq))
     assert got["stats"]["rounds"] == exp.rounds
     assert got["stats"]["seed_edges"] == exp.seed_edges
+    assert got["stats"]["mst_weight"] == device_order_weight(exp.wsq)
 
 
 CASES = ["blobs_d2", "blobs_d10", "blobs_d50", "moons_leaf", "varying_density",
