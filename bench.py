@@ -145,17 +145,22 @@ def measured_peaks():
     return 1900.0, 6800.0, "fallback"
 
 
-# DRAM bytes per launch of the dominant kernel (mean over the Borůvka screen launches of one
-# fit), from the one-pass ncu capture summarised in profiles/screen_dram_vmf500k_d128.md.
-NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": 1783891968.0}
+# DRAM bytes (read + write) per launch of each screen kernel, from the one-pass ncu capture
+# summarised in profiles/screen_dram_vmf500k_d128.md: the kNN sweep (one launch per fit) and
+# the mean over the Borůvka screen launches of one fit.
+NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_sweep": 138863933184.0,
+                                              "boruvka_candidates": 792814272.0}}
+NCU_TRAFFIC_SCOPE = {"knn_sweep": "ncu dram read+write bytes of the kNN screen launch",
+                     "boruvka_candidates": "ncu dram read+write bytes, mean per Borůvka screen "
+                                           "launch"}
 
 
-def ncu_traffic(workload: str, precision: str, n_override):
-    """DRAM bytes per launch of the dominant kernel measured by ncu for this workload (at its
-    own size), if any."""
+def ncu_traffic(workload: str, precision: str, n_override, kernel: str):
+    """DRAM bytes per launch of `kernel` measured by ncu for this workload (at its own size),
+    if any."""
     if n_override is not None:
         return None
-    return NCU_TRAFFIC.get(f"{workload}:{precision}")
+    return NCU_TRAFFIC.get(f"{workload}:{precision}", {}).get(kernel)
 
 
 def cpu_baseline(x: np.ndarray, ms: int, cross_pairs: float, target_s: float) -> dict:
@@ -598,14 +603,16 @@ def run_ours(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.fit_core_device(xd.data_ptr(), n, d, ms, _lib.PRECISION_PLAIN, ids.data_ptr(),
-                            ksq.data_ptr(), core.data_ptr(), src.data_ptr(), dst.data_ptr(),
-                            wsq.data_ptr(), ctx.stream)
+        _, st32 = ctx.fit_core_device(xd.data_ptr(), n, d, ms, _lib.PRECISION_PLAIN,
+                                      ids.data_ptr(), ksq.data_ptr(), core.data_ptr(),
+                                      src.data_ptr(), dst.data_ptr(), wsq.data_ptr(), ctx.stream)
         e1.record(stream)
         e1.synchronize()
         f_ms = e0.elapsed_time(e1)
         fp32 = {"value": n / (f_ms / 1e3) / 1e6, "unit": "Mpts/s", "ms_per_step": f_ms,
-                "steps": 1, f"{args.precision}_speedup": f_ms / ms_per_step}
+                "steps": 1, f"{args.precision}_speedup": f_ms / ms_per_step,
+                # both forms emit the same edge list, so the f64 totals are the same bits
+                "mst_weight_f64_equal": st32.mst_weight == stats["mst_weight"]}
 
     # roofline of the dominant kernel (CUDA events inside the fit, on its stream)
     bf16_peak, hbm_peak, peak_src = measured_peaks()
@@ -619,10 +626,10 @@ def run_ours(args):
         achieved, t_dom, w_dom = w_cand / t_cand / 1e12, t_cand, w_cand
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": bf16_peak,
             "unit": "TFLOP/s", "frac": achieved / bf16_peak, "peak_source": f"{peak_src} bf16",
-            "traffic": ncu_traffic(args.workload, args.precision, args.n),
+            "traffic": ncu_traffic(args.workload, args.precision, args.n, dom),
             "kernel_ms": t_dom * 1e3, "algorithmic_tflop": w_dom / 1e12}
     if roof["traffic"] is not None:
-        roof["traffic_scope"] = "ncu dram read+write bytes, mean per Borůvka screen launch"
+        roof["traffic_scope"] = NCU_TRAFFIC_SCOPE[dom]
     if args.precision != "fp32":
         d_pad = -(-d // 64) * 64
         tiles = int(stats["screen_tile_pairs"])
@@ -658,6 +665,7 @@ def run_ours(args):
                    "boruvka_fallback_rows": stats["boruvka_fallback_rows"],
                    "rescreened_rows": stats["rescreened_rows"],
                    "boruvka_screened_rows": stats["boruvka_screened_rows"],
+                   "mst_weight_f64": stats["mst_weight"],
                    "algorithmic_tflop_per_step": (w_knn + w_cand) / 1e12},
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_pts_per_s / 1e6, "unit": "Mpts/s",
