@@ -49,6 +49,7 @@ SIGNATURES = {
                                   _F32P, _F32P, _U32P, _U32P, _F32P, _I64P, _VP]),
     "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                          _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
+    "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_clusters_from_spanning_tree": (C.c_int, [_U32P, _U32P, _F64P, C.c_int64, _VP,
                                                      C.POINTER(_VP), C.c_char_p, C.c_size_t]),
@@ -93,6 +94,7 @@ SIGNATURES = {
     "cuscan_server_request_error": (C.c_int, [_VP, C.c_int64, C.c_char_p, C.c_size_t]),
     "cuscan_server_release": (C.c_int, [_VP, C.c_int64]),
     "cuscan_server_get_stats": (C.c_int, [_VP, _VP]),
+    "cuscan_server_set_pack_limit": (C.c_int, [_VP, C.c_int32]),
 }
 
 
@@ -119,6 +121,30 @@ class FitStats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+PACK_MAX_FITS = 16
+PACK_MAX_ROWS = 2047
+
+
+class FitItem(C.Structure):
+    """One point set of cuscan_fit_core_packed (host pointers)."""
+    _fields_ = [
+        ("data", _F32P),
+        ("n", C.c_int64),
+        ("d", C.c_int32),
+        ("min_samples", C.c_int32),
+        ("precision", C.c_int32),
+        ("status", C.c_int32),
+        ("knn_ids", _I32P),
+        ("knn_sq", _F32P),
+        ("core_sq", _F32P),
+        ("mst_src", _U32P),
+        ("mst_dst", _U32P),
+        ("mst_wsq", _F32P),
+        ("n_edges", C.c_int64),
+        ("stats", FitStats),
+    ]
+
+
 class ExtractConfig(C.Structure):
     _fields_ = [
         ("min_cluster_size", C.c_int64),
@@ -136,7 +162,7 @@ class ServerInfo(C.Structure):
         ("status", C.c_int32),
         ("slot", C.c_int32),
         ("kind", C.c_int32),
-        ("pad", C.c_int32),
+        ("pack_size", C.c_int32),
         ("n", C.c_int64),
         ("finite_rows", C.c_int64),
         ("d", C.c_int32),
@@ -173,6 +199,8 @@ class ServerStats(C.Structure):
         ("committed_bytes", C.c_int64),
         ("peak_committed_bytes", C.c_int64),
         ("workspace_releases", C.c_int64),
+        ("packs", C.c_int64),
+        ("packed_requests", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -338,6 +366,42 @@ class Context:
         e = int(m.value)
         return {"knn_ids": ids, "knn_sq": ksq, "core_sq": core, "src": src[:e], "dst": dst[:e],
                 "wsq": w[:e], "stats": stats.as_dict()}
+
+
+    def fit_core_packed(self, fits):
+        """Fit cores of several small point sets in one CUDA graph launch.
+
+        `fits` is a sequence of (x, min_samples, precision). Returns one dict per fit, shaped
+        like fit_core's, plus its "status"; raises if any fit failed (the first failure)."""
+        items = (FitItem * len(fits))()
+        keep = []
+        outs = []
+        for item, (x, ms, prec) in zip(items, fits):
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            n, d = x.shape
+            k = min(int(ms), n - 1)
+            o = {"knn_ids": np.empty((n, k), np.int32), "knn_sq": np.empty((n, k), np.float32),
+                 "core_sq": np.empty(n, np.float32), "src": np.empty(max(n - 1, 1), np.uint32),
+                 "dst": np.empty(max(n - 1, 1), np.uint32),
+                 "wsq": np.empty(max(n - 1, 1), np.float32)}
+            keep.append(x)
+            outs.append(o)
+            item.data = x.ctypes.data_as(_F32P)
+            item.n, item.d, item.min_samples, item.precision = n, d, int(ms), int(prec)
+            item.knn_ids = o["knn_ids"].ctypes.data_as(_I32P)
+            item.knn_sq = o["knn_sq"].ctypes.data_as(_F32P)
+            item.core_sq = o["core_sq"].ctypes.data_as(_F32P)
+            item.mst_src = o["src"].ctypes.data_as(_U32P)
+            item.mst_dst = o["dst"].ctypes.data_as(_U32P)
+            item.mst_wsq = o["wsq"].ctypes.data_as(_F32P)
+        self.check(self._lib.cuscan_fit_core_packed(self.handle, items, len(fits)))
+        for item, o in zip(items, outs):
+            e = int(item.n_edges)
+            for key in ("src", "dst", "wsq"):
+                o[key] = o[key][:e]
+            o["stats"] = item.stats.as_dict()
+            o["status"] = int(item.status)
+        return outs
 
 
 def clusters_from_spanning_tree(src, dst, weight, *, min_cluster_size: int,

@@ -93,6 +93,7 @@ void cuscan_ctx_destroy(cuscan_ctx *ctx) {
         const int count = workspace_buffers(f, all);
         for (int i = 0; i < count; ++i) release(*all[i]);
         f->forest.status = nullptr;
+        pack_destroy(f->pack);
         if (f->host_status) cudaFreeHost(f->host_status);
         for (auto &ev : f->ev)
             if (ev) cudaEventDestroy(ev);
@@ -108,7 +109,7 @@ int64_t cuscan_ctx_reserved_bytes(const cuscan_ctx *ctx) {
     const int count = workspace_buffers(ctx->fit, all);
     int64_t total = 0;
     for (int i = 0; i < count; ++i) total += (int64_t)all[i]->bytes;
-    return total;
+    return total + pack_reserved_bytes(ctx->fit->pack);
 }
 
 int cuscan_ctx_release_workspace(cuscan_ctx *ctx) {
@@ -120,6 +121,7 @@ int cuscan_ctx_release_workspace(cuscan_ctx *ctx) {
     const int count = workspace_buffers(ctx->fit, all);
     for (int i = 0; i < count; ++i) release(*all[i]);
     ctx->fit->forest.status = nullptr;
+    pack_release(ctx->fit->pack);
     return CUSCAN_OK;
 }
 

@@ -180,6 +180,10 @@ int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const
                           Buffer &scratch_ids, Buffer &scratch_dist,
                           const int32_t *qmap = nullptr);
 
+// Elements of each split-kNN partial list buffer (ids and distances) that launch_exact_knn_fp32
+// uses for nq queries against nr references (0 when the reference range is not split).
+size_t exact_knn_scratch_elems(const cuscan_ctx *ctx, int64_t nq, int64_t nr, int k);
+
 // Borůvka candidates (boruvka.cu): per-row 64-bit keys (weight bits << 32 | reference id),
 // minimised atomically into row_keys[] (which the caller fills with ~0 first). Rows are
 // positions in `data`; ids maps a position to the original id used for tie-breaking and

@@ -13,6 +13,12 @@ struct DevStatus {
     int err_kind;          // 0 ok, 1 numerical weight, 2 index out of range, 4 no progress
     int pad[3];
     double mst_weight;     // f64 total MST weight, written once after the last round
+    // kept on the device by fits whose round loop runs inside a CUDA graph (no host read
+    // between rounds): the seed's results, rounds run and ordered cross pairs entering them
+    unsigned long long seed_edges;
+    unsigned long long components_after_seed;
+    unsigned long long rounds;
+    double cross_pairs;
 };
 
 // Buffers of the bf16 screening path (refined.cu).

@@ -277,22 +277,30 @@ __global__ void __launch_bounds__(QB) knn_fp32_wide_kernel(
     }
 }
 
-template <int K>
-int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, int64_t nr, int d,
-            int k, int exclude_self, int64_t query_offset, int squared, int32_t *ids, float *dist,
-            cudaStream_t s, Buffer &scratch_ids, Buffer &scratch_dist, const int32_t *qmap) {
-    const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
+// Split the reference range when the query blocks alone cannot fill the GPU: `splits` CTAs per
+// query block, each over `chunk` references.
+void knn_split_plan(const cuscan_ctx *ctx, int64_t nq, int64_t nr, int64_t &splits,
+                    int64_t &chunk) {
     const int64_t qblocks = ceil_div(nq, QB);
-    // Split the reference range when the query blocks alone cannot fill the GPU.
-    int64_t splits = 1;
+    splits = 1;
     const int64_t target = 2 * (int64_t)ctx->sm_count;
     if (qblocks < target) splits = ceil_div(target, qblocks);
     const int64_t max_splits = ceil_div(nr, (int64_t)RT * 8);
     if (splits > max_splits) splits = max_splits;
     if (splits > 1024) splits = 1024;
     if (splits < 1) splits = 1;
-    int64_t chunk = ceil_div(ceil_div(nr, splits), RT) * RT;
+    chunk = ceil_div(ceil_div(nr, splits), RT) * RT;
     splits = ceil_div(nr, chunk);
+}
+
+template <int K>
+int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, int64_t nr, int d,
+            int k, int exclude_self, int64_t query_offset, int squared, int32_t *ids, float *dist,
+            cudaStream_t s, Buffer &scratch_ids, Buffer &scratch_dist, const int32_t *qmap) {
+    const float pad = squared ? std::numeric_limits<float>::infinity() : 3.40282346638528859812e+38f;
+    const int64_t qblocks = ceil_div(nq, QB);
+    int64_t splits = 1, chunk = 0;
+    knn_split_plan(ctx, nq, nr, splits, chunk);
     const size_t smem = ((size_t)d * QB + 2 * (size_t)d * RTP) * sizeof(float);
     if (int rc = allow_dynamic_smem(ctx, knn_fp32_kernel<K>, smem)) return rc;
     dim3 grid((unsigned)qblocks, (unsigned)splits);
@@ -324,6 +332,12 @@ int run_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref, i
 }
 
 }  // namespace
+
+size_t exact_knn_scratch_elems(const cuscan_ctx *ctx, int64_t nq, int64_t nr, int k) {
+    int64_t splits = 1, chunk = 0;
+    knn_split_plan(ctx, nq, nr, splits, chunk);
+    return splits > 1 ? (size_t)(nq * k * splits) : 0;
+}
 
 int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const float *ref,
                           int64_t nr, int d, int k, int exclude_self, int64_t query_offset,

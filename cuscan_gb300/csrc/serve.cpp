@@ -13,6 +13,12 @@
 // CUSCAN_MEMORY at once. The queue is first in, first out: a request that does not fit is
 // never overtaken, so no request starves.
 //
+// Small fits are packed: a slot that admits a fit of at most CUSCAN_PACK_MAX_ROWS rows at the
+// head of the queue also takes the small fits queued right behind it (in order, up to the pack
+// limit, while the budget allows) and runs them in one CUDA graph launch
+// (cuscan_fit_core_packed). A pack commits the sum of its requests' bounds on top of the
+// workspace the slot holds, since its fits use buffers of their own.
+//
 // A request runs the estimator flow of crates/hdbscan/src/estimator.rs:1034-1392 for one
 // point set: non-finite rows are set aside (crates/hdbscan-core/src/finite.rs:65-131), the
 // fit core runs on the finite rows (cuscan_fit_core), and the host extraction
@@ -64,6 +70,7 @@ struct Request {
     Clock::time_point t_submit, t_admit, t_done;
     double prep_ms = 0, fit_ms = 0, extract_ms = 0;  // host wall time of the three phases
     int slot = -1;
+    int32_t pack_size = 1;
     bool done = false;
     int status = CUSCAN_OK;
     std::string error;
@@ -85,9 +92,10 @@ struct Slot {
     int index = 0;
     cuscan_ctx *ctx = nullptr;
     int64_t reserved = 0;   // workspace held (bytes)
-    int64_t running = 0;    // admission bound of the request it runs
+    int64_t running = 0;    // admission bound of the request it runs (sum over a pack)
     Task task = Task::None;
     Request *req = nullptr;
+    std::vector<Request *> pack;  // two or more small fits run in one graph launch
     std::condition_variable cv;
 };
 
@@ -96,12 +104,16 @@ struct Slot {
 struct Executor {
     virtual ~Executor() = default;
     virtual void run(Slot &slot, Request &r) = 0;
+    virtual void run_pack(Slot &slot, std::vector<Request *> &pack) {
+        for (Request *r : pack) run(slot, *r);
+    }
     virtual void release(Slot &slot) = 0;
     virtual int64_t reserved(Slot &slot) = 0;
 };
 
 struct DeviceExecutor : Executor {
     void run(Slot &slot, Request &r) override;
+    void run_pack(Slot &slot, std::vector<Request *> &pack) override;
     void predict(Slot &slot, Request &r);
     void release(Slot &slot) override { cuscan_ctx_release_workspace(slot.ctx); }
     int64_t reserved(Slot &slot) override { return cuscan_ctx_reserved_bytes(slot.ctx); }
@@ -137,67 +149,68 @@ void DeviceExecutor::predict(Slot &slot, Request &r) {
     if (rc) r.error = cuscan_last_error(slot.ctx);
 }
 
-void DeviceExecutor::run(Slot &slot, Request &r) {
-    if (r.kind == Kind::Predict) {
-        predict(slot, r);
-        return;
-    }
-    const Clock::time_point t0 = Clock::now();
+// The finite rows of a fit request (finite.rs:65-131): their original indices and, when some
+// rows are set aside, a compact copy. Prepares the request's outputs (-1 / 0 for every row).
+struct FiniteRows {
+    std::vector<int64_t> index;
+    std::vector<float> compact;
+    const float *x = nullptr;
+    int64_t n = 0;
+};
+
+void split_finite(Request &r, FiniteRows &f) {
     const int64_t n = r.n;
     const int32_t d = r.d;
-    // finite split (finite.rs:65-131)
-    std::vector<int64_t> finite;
-    finite.reserve((size_t)n);
+    f.index.clear();
+    f.index.reserve((size_t)n);
     for (int64_t i = 0; i < n; ++i) {
         const float *row = r.x + i * d;
         bool ok = true;
-        for (int32_t f = 0; f < d; ++f)
-            if (!std::isfinite(row[f])) {
+        for (int32_t c = 0; c < d; ++c)
+            if (!std::isfinite(row[c])) {
                 ok = false;
                 break;
             }
-        if (ok) finite.push_back(i);
+        if (ok) f.index.push_back(i);
     }
-    const int64_t nf = (int64_t)finite.size();
-    r.finite_rows = nf;
-    std::vector<float> compact;
-    const float *xf = r.x;
-    if (nf != n) {
-        compact.resize((size_t)nf * d);
-        for (int64_t i = 0; i < nf; ++i)
-            std::memcpy(compact.data() + i * d, r.x + finite[i] * d, sizeof(float) * d);
-        xf = compact.data();
+    f.n = (int64_t)f.index.size();
+    r.finite_rows = f.n;
+    f.x = r.x;
+    if (f.n != n) {
+        f.compact.resize((size_t)f.n * d);
+        for (int64_t i = 0; i < f.n; ++i)
+            std::memcpy(f.compact.data() + i * d, r.x + f.index[(size_t)i] * d,
+                        sizeof(float) * d);
+        f.x = f.compact.data();
     }
     r.labels.assign((size_t)n, -1);
     r.probabilities.assign((size_t)n, 0.0f);
-    r.core.assign((size_t)nf, INFINITY);
+    r.core.assign((size_t)f.n, INFINITY);
     r.sorted_mst.clear();
-    if (nf < 2) {  // one finite row or none: all noise, empty trees (hdbscan-core lib.rs:40-50)
-        r.status = CUSCAN_OK;
-        return;
+}
+
+// Fit-core outputs of one request, and the host extraction that turns them into labels.
+struct CoreOutputs {
+    std::vector<float> core_sq, wsq;
+    std::vector<uint32_t> src, dst;
+    void size_for(int64_t nf) {
+        core_sq.resize((size_t)nf);
+        wsq.resize((size_t)(nf - 1));
+        src.resize((size_t)(nf - 1));
+        dst.resize((size_t)(nf - 1));
     }
-    const int64_t m = nf - 1;
-    std::vector<float> core_sq((size_t)nf), wsq((size_t)m);
-    std::vector<uint32_t> src((size_t)m), dst((size_t)m);
-    int64_t edges = 0;
-    const Clock::time_point t1 = Clock::now();
-    r.prep_ms = ms_between(t0, t1);
-    int rc = cuscan_fit_core(slot.ctx, xf, nf, d, r.min_samples, r.precision, nullptr, nullptr,
-                             core_sq.data(), src.data(), dst.data(), wsq.data(), &edges, &r.stats);
-    const Clock::time_point t2 = Clock::now();
-    r.fit_ms = ms_between(t1, t2);
-    if (rc) {
-        r.status = rc;
-        r.error = cuscan_last_error(slot.ctx);
-        return;
-    }
-    for (int64_t i = 0; i < nf; ++i) r.core[(size_t)i] = std::sqrt(core_sq[(size_t)i]);
+};
+
+void finish(Request &r, const FiniteRows &f, const CoreOutputs &o) {
+    const Clock::time_point t0 = Clock::now();
+    const int64_t nf = f.n, m = nf - 1;
+    for (int64_t i = 0; i < nf; ++i) r.core[(size_t)i] = std::sqrt(o.core_sq[(size_t)i]);
     std::vector<double> w((size_t)m);
-    for (int64_t e = 0; e < m; ++e) w[(size_t)e] = std::sqrt((double)wsq[(size_t)e]);
+    for (int64_t e = 0; e < m; ++e) w[(size_t)e] = std::sqrt((double)o.wsq[(size_t)e]);
     cuscan_clustering *c = nullptr;
     char err[512] = {0};
-    rc = cuscan_clusters_from_spanning_tree(src.data(), dst.data(), w.data(), m, &r.cfg, &c, err,
-                                            sizeof(err));
+    int rc = cuscan_clusters_from_spanning_tree(o.src.data(), o.dst.data(), w.data(), m, &r.cfg,
+                                                &c, err, sizeof(err));
     if (rc) {
         r.status = rc;
         r.error = err;
@@ -211,13 +224,95 @@ void DeviceExecutor::run(Slot &slot, Request &r) {
     cuscan_clustering_free(c);
     int32_t top = -1;
     for (int64_t i = 0; i < nf; ++i) {
-        r.labels[(size_t)finite[(size_t)i]] = lab[(size_t)i];
-        r.probabilities[(size_t)finite[(size_t)i]] = prob[(size_t)i];
+        r.labels[(size_t)f.index[(size_t)i]] = lab[(size_t)i];
+        r.probabilities[(size_t)f.index[(size_t)i]] = prob[(size_t)i];
         top = std::max(top, lab[(size_t)i]);
     }
     r.clusters = top + 1;
     r.status = CUSCAN_OK;
-    r.extract_ms = ms_between(t2, Clock::now());
+    r.extract_ms = ms_between(t0, Clock::now());
+}
+
+void DeviceExecutor::run(Slot &slot, Request &r) {
+    if (r.kind == Kind::Predict) {
+        predict(slot, r);
+        return;
+    }
+    const Clock::time_point t0 = Clock::now();
+    FiniteRows f;
+    split_finite(r, f);
+    if (f.n < 2) {  // one finite row or none: all noise, empty trees (hdbscan-core lib.rs:40-50)
+        r.status = CUSCAN_OK;
+        return;
+    }
+    CoreOutputs o;
+    o.size_for(f.n);
+    int64_t edges = 0;
+    const Clock::time_point t1 = Clock::now();
+    r.prep_ms = ms_between(t0, t1);
+    int rc = cuscan_fit_core(slot.ctx, f.x, f.n, r.d, r.min_samples, r.precision, nullptr,
+                             nullptr, o.core_sq.data(), o.src.data(), o.dst.data(), o.wsq.data(),
+                             &edges, &r.stats);
+    r.fit_ms = ms_between(t1, Clock::now());
+    if (rc) {
+        r.status = rc;
+        r.error = cuscan_last_error(slot.ctx);
+        return;
+    }
+    finish(r, f, o);
+}
+
+// Small fits of one pack: finite split of each, one graph launch for all fit cores, then the
+// extraction of each.
+void DeviceExecutor::run_pack(Slot &slot, std::vector<Request *> &pack) {
+    const size_t count = pack.size();
+    std::vector<FiniteRows> f(count);
+    std::vector<CoreOutputs> o(count);
+    std::vector<cuscan_fit_item> items;
+    std::vector<size_t> owner;  // request of each item
+    items.reserve(count);
+    for (size_t i = 0; i < count; ++i) {
+        Request &r = *pack[i];
+        const Clock::time_point t0 = Clock::now();
+        split_finite(r, f[i]);
+        r.prep_ms = ms_between(t0, Clock::now());
+        if (f[i].n < 2) {
+            r.status = CUSCAN_OK;
+            continue;
+        }
+        o[i].size_for(f[i].n);
+        cuscan_fit_item it;
+        std::memset(&it, 0, sizeof(it));
+        it.data = f[i].x;
+        it.n = f[i].n;
+        it.d = r.d;
+        it.min_samples = r.min_samples;
+        it.precision = r.precision;
+        it.core_sq = o[i].core_sq.data();
+        it.mst_src = o[i].src.data();
+        it.mst_dst = o[i].dst.data();
+        it.mst_wsq = o[i].wsq.data();
+        items.push_back(it);
+        owner.push_back(i);
+    }
+    if (items.empty()) return;
+    const Clock::time_point t1 = Clock::now();
+    const int rc = cuscan_fit_core_packed(slot.ctx, items.data(), (int32_t)items.size());
+    const double fit_ms = ms_between(t1, Clock::now());
+    const std::string msg = rc ? cuscan_last_error(slot.ctx) : std::string();
+    for (size_t j = 0; j < items.size(); ++j) {
+        Request &r = *pack[owner[j]];
+        r.fit_ms = fit_ms;
+        r.stats = items[j].stats;
+        // a call-wide failure (CUDA error, rejected pack) leaves the item statuses at OK
+        const int st = items[j].status ? items[j].status : rc;
+        if (st) {
+            r.status = st;
+            r.error = msg;
+            continue;
+        }
+        finish(r, f[owner[j]], o[owner[j]]);
+    }
 }
 
 }  // namespace
@@ -237,13 +332,25 @@ struct cuscan_server {
     int64_t next_id = 1;
     int64_t submitted = 0, completed = 0, failed = 0, releases = 0;
     int64_t peak_committed = 0;
+    int32_t pack_limit = 8;
+    int64_t packs = 0, packed_requests = 0;
     Clock::time_point t0 = Clock::now();
     bool stopping = false;
 
+    // A slot commits the larger of what it holds and what its request may grow it to; a pack
+    // runs on buffers of its own, so it commits its bounds on top of what the slot holds.
+    static int64_t commitment(const Slot &s) {
+        return s.pack.empty() ? std::max(s.reserved, s.running) : s.reserved + s.running;
+    }
+
     int64_t committed_locked() const {
         int64_t total = 0;
-        for (auto &s : slots) total += std::max(s->reserved, s->running);
+        for (auto &s : slots) total += commitment(*s);
         return total;
+    }
+
+    static bool small_fit(const Request *r) {
+        return r->kind == Kind::Fit && r->n <= CUSCAN_PACK_MAX_ROWS;
     }
 
     // Admit queued requests onto idle slots while the budget allows (called with mu held).
@@ -263,7 +370,7 @@ struct cuscan_server {
                 }
             }
             if (!best) return;  // every slot is busy
-            const int64_t others = committed_locked() - std::max(best->reserved, best->running);
+            const int64_t others = committed_locked() - commitment(*best);
             if (others + std::max(best->reserved, r->bytes) <= budget) {
                 queue.pop_front();
                 best->task = Task::Fit;
@@ -271,6 +378,28 @@ struct cuscan_server {
                 best->running = r->bytes;
                 r->slot = index_of(best);
                 r->t_admit = Clock::now();
+                // small fits queued right behind a small head join it in one graph launch
+                if (small_fit(r) && pack_limit > 1) {
+                    int64_t sum = r->bytes;
+                    std::vector<Request *> pack{r};
+                    while (!queue.empty() && (int)pack.size() < pack_limit &&
+                           small_fit(queue.front()) &&
+                           others + best->reserved + sum + queue.front()->bytes <= budget) {
+                        Request *q = queue.front();
+                        queue.pop_front();
+                        q->slot = r->slot;
+                        q->t_admit = r->t_admit;
+                        sum += q->bytes;
+                        pack.push_back(q);
+                    }
+                    if (pack.size() > 1) {
+                        for (Request *q : pack) q->pack_size = (int32_t)pack.size();
+                        best->pack = std::move(pack);
+                        best->running = sum;
+                        ++packs;
+                        packed_requests += (int64_t)best->pack.size();
+                    }
+                }
                 peak_committed = std::max(peak_committed, committed_locked());
                 best->cv.notify_one();
                 continue;
@@ -302,28 +431,36 @@ struct cuscan_server {
         for (;;) {
             Task task;
             Request *r;
+            std::vector<Request *> pack;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 slot.cv.wait(lk, [&] { return slot.task != Task::None; });
                 task = slot.task;
                 r = slot.req;
+                pack = slot.pack;
             }
             if (task == Task::Stop) return;
-            if (task == Task::Fit) exec->run(slot, *r);
+            if (task == Task::Fit && !pack.empty()) exec->run_pack(slot, pack);
+            else if (task == Task::Fit) exec->run(slot, *r);
             else exec->release(slot);
+            if (pack.empty() && task == Task::Fit) pack.push_back(r);
             const int64_t held = exec->reserved(slot);
             {
                 std::lock_guard<std::mutex> lk(mu);
                 slot.reserved = held;
                 slot.running = 0;
                 slot.req = nullptr;
+                slot.pack.clear();
                 if (slot.task != Task::Stop) slot.task = Task::None;
                 if (task == Task::Fit) {
-                    r->t_done = Clock::now();
-                    r->done = true;
-                    ++completed;
-                    if (r->status) ++failed;
-                    finished.push_back(r->id);
+                    const Clock::time_point now = Clock::now();
+                    for (Request *q : pack) {
+                        q->t_done = now;
+                        q->done = true;
+                        ++completed;
+                        if (q->status) ++failed;
+                        finished.push_back(q->id);
+                    }
                 }
                 schedule_locked();
             }
@@ -360,6 +497,7 @@ struct cuscan_server {
         std::memset(info, 0, sizeof(*info));
         info->request_id = r.id;
         info->kind = (int32_t)r.kind;
+        info->pack_size = r.pack_size;
         info->status = r.done ? r.status : CUSCAN_PENDING;
         info->slot = r.slot;
         info->n = r.n;
@@ -612,6 +750,16 @@ int cuscan_server_get_stats(cuscan_server *s, cuscan_server_stats *out) {
     out->committed_bytes = s->committed_locked();
     out->peak_committed_bytes = s->peak_committed;
     out->workspace_releases = s->releases;
+    out->packs = s->packs;
+    out->packed_requests = s->packed_requests;
+    return CUSCAN_OK;
+}
+
+int cuscan_server_set_pack_limit(cuscan_server *s, int32_t max_fits) {
+    if (!s) return CUSCAN_INVALID_INPUT;
+    if (max_fits < 1 || max_fits > CUSCAN_PACK_MAX_FITS) return CUSCAN_INVALID_CONFIG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->pack_limit = max_fits;
     return CUSCAN_OK;
 }
 

@@ -6,6 +6,12 @@
 
 namespace cuscan {
 
+// Workspace of packed small fits (pack.cu): per-fit buffers, branch streams, pinned staging.
+struct PackWorkspace;
+int64_t pack_reserved_bytes(const PackWorkspace *p);  // device bytes held
+void pack_release(PackWorkspace *p);                 // frees device and pinned buffers
+void pack_destroy(PackWorkspace *p);                 // also streams and events
+
 struct FitWorkspace {
     ForestBuffers forest;
     Buffer x, ids, dsq, core, label, src, dst, w;  // device copies for the host-pointer entry
@@ -13,6 +19,7 @@ struct FitWorkspace {
     Buffer pred_q, pred_ids, pred_dist;            // approximate_predict queries and candidates
     DevStatus *host_status = nullptr;              // pinned
     cudaEvent_t ev[6] = {};
+    PackWorkspace *pack = nullptr;                 // created by the first packed call
 };
 constexpr int kOwnBufferCount = 17;
 

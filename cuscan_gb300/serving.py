@@ -30,11 +30,14 @@ def _precision_code(precision: str) -> int:
 class FitServer:
     """Fit-request server. ``budget_bytes`` bounds the device workspace of all slots together.
 
+    ``pack_limit`` is the most small fits (at most ``_lib.PACK_MAX_ROWS`` rows) a slot runs
+    together in one CUDA graph launch; 1 runs every fit on its own.
+
     ``simulated_us_per_kpoint`` builds the scheduling test double instead: the same queue and
     admission with slots that run no fit (no GPU needed; results cannot be read)."""
 
     def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 16 << 30, *,
-                 simulated_us_per_kpoint: float | None = None):
+                 pack_limit: int = 8, simulated_us_per_kpoint: float | None = None):
         self._lib = _lib.load()
         handle = C.c_void_p()
         err = C.create_string_buffer(256)
@@ -47,6 +50,10 @@ class FitServer:
                                                             C.byref(handle), err, 256)
         _lib.raise_for(code, err.value.decode("utf-8", "replace") or
                        f"could not start a fit server on device {device}")
+        code = self._lib.cuscan_server_set_pack_limit(handle, int(pack_limit))
+        if code != _lib.OK:
+            self._lib.cuscan_server_destroy(handle)
+            _lib.raise_for(code, f"pack_limit must be 1 to {_lib.PACK_MAX_FITS}")
         self.handle = handle
         self.simulated = simulated_us_per_kpoint is not None
         self._inputs: dict[int, np.ndarray] = {}

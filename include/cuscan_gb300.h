@@ -192,6 +192,41 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
                            void *stream);
 
 /*
+ * Packed small fits (no reference counterpart; each fit is the core_distances + spanning_tree
+ * body of crates/hdbscan/src/estimator.rs:524-874, as in cuscan_fit_core). Up to
+ * CUSCAN_PACK_MAX_FITS independent point sets of at most CUSCAN_PACK_MAX_ROWS rows each are fit
+ * in ONE CUDA graph launch: the graph holds one branch per fit (copy in, exact kNN, core
+ * distances, kNN seed, the Borůvka rounds as a device-controlled while loop, f64 MST weight,
+ * copy out), so the fits overlap on the device and no host round trip happens between rounds.
+ * At these sizes every precision runs the exact f32 kernels, so each item's outputs are bit
+ * identical to cuscan_fit_core's for the same input. The graph is captured and instantiated on
+ * every call. Host pointers; the call synchronises the context stream before returning.
+ * Each item's status is set; the call returns the first failing item's status (message in
+ * cuscan_last_error), or CUSCAN_OK. Stats: core_ms covers the copy in, the kNN sweep and the
+ * core column of the item's branch, mst_ms the seed, the rounds, the weight and the copy out;
+ * candidate_kernel_ms is 0 (the rounds are not timed one by one).
+ */
+#define CUSCAN_PACK_MAX_FITS 16
+#define CUSCAN_PACK_MAX_ROWS 2047
+typedef struct cuscan_fit_item {
+    const float *data;      /* host, n x d row-major, finite */
+    int64_t n;              /* 2 .. CUSCAN_PACK_MAX_ROWS */
+    int32_t d;              /* 1 .. 256 */
+    int32_t min_samples;
+    int32_t precision;      /* a cuscan_precision */
+    int32_t status;         /* out: cuscan_status of this fit */
+    int32_t *knn_ids;       /* host out, n*k (k = min(min_samples, n-1)); may be NULL */
+    float *knn_sq;          /* host out, n*k; may be NULL */
+    float *core_sq;         /* host out, n */
+    uint32_t *mst_src;      /* host out, n-1 edges in the reference's merge order */
+    uint32_t *mst_dst;
+    float *mst_wsq;
+    int64_t n_edges;        /* out */
+    cuscan_fit_stats stats; /* out */
+} cuscan_fit_item;
+int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, int32_t count);
+
+/*
  * Diagnostic of the bf16 tensor-core screen (no reference counterpart): runs the screening
  * pipeline on `data` (device, n >= 256 rows) and writes the raw fp32 accumulator of the first
  * 128-row query block against the first 256-row reference tile, i.e. the bf16 dot products
@@ -355,7 +390,7 @@ typedef struct cuscan_server_info {
     int32_t status;          /* outcome once finished; CUSCAN_PENDING while queued or running */
     int32_t slot;            /* slot that ran it, -1 before admission */
     int32_t kind;            /* 0 fit, 1 approximate_predict */
-    int32_t pad;
+    int32_t pack_size;       /* fits in the graph launch that ran it (1: run on its own) */
     int64_t n;
     int64_t finite_rows;
     int32_t d;
@@ -380,6 +415,8 @@ typedef struct cuscan_server_stats {
     int64_t committed_bytes;       /* current sum of slot commitments */
     int64_t peak_committed_bytes;  /* largest sum at any admission */
     int64_t workspace_releases;    /* idle-slot releases ordered by admission */
+    int64_t packs;                 /* graph launches that ran two or more small fits */
+    int64_t packed_requests;       /* fit requests those launches ran */
 } cuscan_server_stats;
 
 int cuscan_server_create(int device, int32_t slots, int64_t budget_bytes, cuscan_server **out,
@@ -419,6 +456,12 @@ int cuscan_server_request_error(cuscan_server *server, int64_t request_id, char 
 /* Drop a finished request's results. */
 int cuscan_server_release(cuscan_server *server, int64_t request_id);
 int cuscan_server_get_stats(cuscan_server *server, cuscan_server_stats *out);
+/* Most small fits (at most CUSCAN_PACK_MAX_ROWS rows) one slot runs together in one graph
+ * launch (cuscan_fit_core_packed), 1 .. CUSCAN_PACK_MAX_FITS; 1 turns packing off. When a
+ * slot admits a small fit at the head of the queue it also takes the small fits queued right
+ * behind it, in order, while the pack limit and the memory budget allow (a pack commits the
+ * sum of its requests' bounds on top of the workspace the slot holds). Default 8. */
+int cuscan_server_set_pack_limit(cuscan_server *server, int32_t max_fits);
 
 #ifdef __cplusplus
 }

@@ -109,6 +109,51 @@ def test_invalid_server_and_request_arguments():
             assert srv.wait(rid, 5.0)["status"] == _lib.OK
 
 
+def test_small_fits_behind_a_small_head_run_as_one_pack():
+    with FitServer(slots=1, budget_bytes=1 << 34, pack_limit=8,
+                   simulated_us_per_kpoint=2000.0) as srv:
+        blocker = srv.submit(np.zeros((20000, 8), np.float32))  # occupies the slot ~40 ms
+        sizes = [1000] * 10 + [30000] + [500] * 3
+        ids = [srv.submit(np.zeros((n, 8), np.float32)) for n in sizes]
+        infos = drain(srv, [blocker] + ids)
+        st = srv.stats()
+    packs = [infos[r]["pack_size"] for r in ids]
+    # the first eight small fits form one pack, the next two a second one (the large request
+    # behind them is never overtaken), the last three a third one
+    assert packs == [8] * 8 + [2] * 2 + [1] + [3] * 3, packs
+    assert st["packs"] == 3 and st["packed_requests"] == 13
+    assert infos[blocker]["pack_size"] == 1
+    admitted = [infos[r]["submit_ms"] + infos[r]["queued_ms"] for r in ids]
+    assert all(b >= a - 1e-6 for a, b in zip(admitted, admitted[1:])), "admission out of order"
+    assert len({infos[r]["slot"] for r in ids[:8]}) == 1
+
+
+def test_pack_stays_within_the_budget():
+    small = bound(2000, 64)
+    budget = 3 * small + (1 << 20)
+    with FitServer(slots=1, budget_bytes=budget, pack_limit=16,
+                   simulated_us_per_kpoint=2000.0) as srv:
+        blocker = srv.submit(np.zeros((2000, 64), np.float32))
+        ids = [srv.submit(np.zeros((2000, 64), np.float32)) for _ in range(9)]
+        infos = drain(srv, [blocker] + ids)
+        st = srv.stats()
+    assert st["peak_committed_bytes"] <= budget
+    assert max(infos[r]["pack_size"] for r in ids) <= 2  # held workspace + two bounds fit
+    assert st["completed"] == 10 and st["failed"] == 0
+
+
+def test_pack_limit_one_runs_every_fit_alone():
+    with FitServer(slots=1, budget_bytes=1 << 34, pack_limit=1,
+                   simulated_us_per_kpoint=2000.0) as srv:
+        ids = [srv.submit(np.zeros((1000, 8), np.float32)) for _ in range(6)]
+        infos = drain(srv, ids)
+        assert srv.stats()["packs"] == 0
+    assert all(infos[r]["pack_size"] == 1 for r in ids)
+    for bad in (0, _lib.PACK_MAX_FITS + 1):
+        with pytest.raises(ValueError):
+            FitServer(slots=1, budget_bytes=1 << 30, pack_limit=bad, simulated_us_per_kpoint=1.0)
+
+
 def host_predictor():
     from cuscan_gb300.prediction import Predictor
     labels = np.array([0, 0, 0, 1, 1, 1], np.int32)
@@ -171,6 +216,36 @@ def test_results_in_the_mix_equal_fits_alone():
         st = srv.stats()
     assert st["completed"] == len(mix) and st["failed"] == 0
     assert max(r["info"]["slot"] for r in results) > 0  # more than one slot was used
+    for m, r in zip(alone, results):
+        np.testing.assert_array_equal(r["labels"], m.labels_)
+        np.testing.assert_array_equal(r["probabilities"].view(np.uint32),
+                                      np.asarray(m.probabilities_, np.float32).view(np.uint32))
+        np.testing.assert_array_equal(r["core_distances"].view(np.uint32),
+                                      np.asarray(m.core_distances_, np.float32).view(np.uint32))
+        np.testing.assert_array_equal(r["minimum_spanning_tree"], m.minimum_spanning_tree_)
+
+
+@pytest.mark.gpu
+def test_packed_small_fits_equal_fits_alone():
+    import cuscan_gb300 as cg
+    rng = np.random.default_rng(33)
+    mix = []
+    for i in range(24):
+        n = int(np.exp(rng.uniform(np.log(40), np.log(2047))))
+        d = int(rng.choice([16, 32, 64, 128]))
+        x = synthetic.gaussian_mixture(n, d, int(rng.integers(2, 30)), seed=500 + i)
+        if i == 5:
+            x[::7, 1] = np.nan  # rows set aside before the packed fit core
+        mix.append((x, max(5, n // 200), ("bf16_refined", "fp16_refined", "fp32")[i % 3]))
+    alone = [cg.HDBSCAN(min_cluster_size=mcs, min_samples=5, precision=prec).fit(x)
+             for x, mcs, prec in mix]
+    with FitServer(slots=2, budget_bytes=8 << 30, pack_limit=8) as srv:
+        ids = [srv.submit(x, min_cluster_size=mcs, min_samples=5, precision=prec)
+               for x, mcs, prec in mix]
+        results = [srv.result(r, timeout=120.0) for r in ids]
+        st = srv.stats()
+    assert st["completed"] == len(mix) and st["failed"] == 0
+    assert st["packs"] > 0 and max(r["info"]["pack_size"] for r in results) > 1
     for m, r in zip(alone, results):
         np.testing.assert_array_equal(r["labels"], m.labels_)
         np.testing.assert_array_equal(r["probabilities"].view(np.uint32),
