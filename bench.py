@@ -330,7 +330,45 @@ def serving_run(args, precision: str) -> dict:
                     "failures": int(fails), "by_size": by_size(recs)},
         "peak_committed_bytes": st["peak_committed_bytes"],
         "workspace_releases": st["workspace_releases"],
+        "packs": st["packs"], "packed_requests": st["packed_requests"],
     }
+
+
+def small_fit_packing_section(args) -> dict:
+    """The small requests of the fit stream (n <= 2047 rows, every d of the stream), all queued
+    at once, run with packing off (pack_limit 1: every fit on its own, about a hundred launches
+    and a host read per round) and on (up to 8 fits per CUDA graph launch). Throughput and
+    latency at saturation for both; the results are the same bits either way (GPU tests)."""
+    import torch
+
+    from cuscan_gb300 import _lib, synthetic
+    from cuscan_gb300.serving import FitServer
+
+    specs = [sp for sp in synthetic.fit_request_stream(args.serve_requests)
+             if sp["n"] <= _lib.PACK_MAX_ROWS][:1000]
+    points = [synthetic.request_points(sp) for sp in specs]
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(0.5 * free)
+    out = {"requests": len(specs), "slots": args.serve_slots, "precision": "fp16_refined"}
+    for limit in (1, 8):
+        with FitServer(slots=args.serve_slots, budget_bytes=budget, pack_limit=limit) as srv:
+            for rep_ in range(2):  # the first pass warms the slots' workspaces
+                t0 = time.perf_counter()
+                ids = [srv.submit(x, min_cluster_size=sp["min_cluster_size"],
+                                  min_samples=sp["min_samples"], precision="fp16_refined")
+                       for x, sp in zip(points, specs)]
+                lat = [srv.wait(r, 300.0)["latency_ms"] for r in ids]
+                span = time.perf_counter() - t0
+                for r in ids:
+                    srv.release(r)
+            st = srv.stats()
+        out[f"pack_limit_{limit}"] = {
+            "req_per_s": len(specs) / span, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "packs": st["packs"],
+            "packed_requests": st["packed_requests"]}
+    out["packing_speedup"] = (out["pack_limit_8"]["req_per_s"] /
+                              out["pack_limit_1"]["req_per_s"])
+    return out
 
 
 def mixed_serving_section(args) -> dict:
@@ -464,6 +502,7 @@ def serving_section(args) -> dict:
            "latency": "arrival -> labels and strengths ready on the host"}
     for prec in args.serve_precisions.split(","):
         out[prec] = serving_run(args, prec)
+    out["small_fit_packing"] = small_fit_packing_section(args)
     if args.mixed_predictors > 0:
         out["mixed"] = mixed_serving_section(args)
     return out

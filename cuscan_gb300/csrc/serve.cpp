@@ -332,7 +332,10 @@ struct cuscan_server {
     int64_t next_id = 1;
     int64_t submitted = 0, completed = 0, failed = 0, releases = 0;
     int64_t peak_committed = 0;
-    int32_t pack_limit = 8;
+    // Off by default: with several slots, building a graph per pack costs more host time
+    // (capture and instantiation, serialised across slot threads) than the slots' ordinary
+    // launches of the same fits overlap away.
+    int32_t pack_limit = 1;
     int64_t packs = 0, packed_requests = 0;
     Clock::time_point t0 = Clock::now();
     bool stopping = false;

@@ -31,13 +31,14 @@ class FitServer:
     """Fit-request server. ``budget_bytes`` bounds the device workspace of all slots together.
 
     ``pack_limit`` is the most small fits (at most ``_lib.PACK_MAX_ROWS`` rows) a slot runs
-    together in one CUDA graph launch; 1 runs every fit on its own.
+    together in one CUDA graph launch; 1 (the default) runs every fit on its own, which is
+    faster when several slots share the host (see ``cuscan_server_set_pack_limit``).
 
     ``simulated_us_per_kpoint`` builds the scheduling test double instead: the same queue and
     admission with slots that run no fit (no GPU needed; results cannot be read)."""
 
     def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 16 << 30, *,
-                 pack_limit: int = 8, simulated_us_per_kpoint: float | None = None):
+                 pack_limit: int = 1, simulated_us_per_kpoint: float | None = None):
         self._lib = _lib.load()
         handle = C.c_void_p()
         err = C.create_string_buffer(256)

@@ -460,7 +460,10 @@ int cuscan_server_get_stats(cuscan_server *server, cuscan_server_stats *out);
  * launch (cuscan_fit_core_packed), 1 .. CUSCAN_PACK_MAX_FITS; 1 turns packing off. When a
  * slot admits a small fit at the head of the queue it also takes the small fits queued right
  * behind it, in order, while the pack limit and the memory budget allow (a pack commits the
- * sum of its requests' bounds on top of the workspace the slot holds). Default 8. */
+ * sum of its requests' bounds on top of the workspace the slot holds). Default 1: with
+ * several slots the host time of building one graph per pack (capture and instantiation,
+ * serialised across slot threads) outweighs what it saves; packing pays when one host thread
+ * issues many small fits. */
 int cuscan_server_set_pack_limit(cuscan_server *server, int32_t max_fits);
 
 #ifdef __cplusplus
