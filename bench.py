@@ -534,7 +534,7 @@ def run_reference(args):
         "ms_per_step": float(np.median(times)) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": args.workload, "n": n, "d": d, "min_samples": ms,
-                   "min_cluster_size": mcs, "parallelism": "replicas",
+                   "min_cluster_size": mcs, "parallelism": "single",
                    "cross_pairs": cross, "cross_pairs_source": cross_note},
         "cpu_baseline": {"value": value, "unit": "Mpts/s", "cores": O.max_threads(),
                          "kind": "port", "sample": cb["sample"]},
