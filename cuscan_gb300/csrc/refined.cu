@@ -1002,7 +1002,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         tmem_ld_wait(rm);
                         if ((mixbits >> c) & 1u) {
                             const int64_t j0 = t * BN + half * HALF + c * 32;
-#pragma unroll 4
+                            // fully unrolled: rm stays in registers
+#pragma unroll
                             for (int e = 0; e < 32; ++e) {
                                 const int col = c * 32 + e;
                                 if (j0 + e >= P.n || P.label[j0 + e] == lab_i) continue;
