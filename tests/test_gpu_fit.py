@@ -245,3 +245,67 @@ def test_large_blobs_fp16_equals_plain(gpu_ctx):
     for key in ("knn_sq", "core_sq", "wsq"):
         np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
     check_tree_properties(x, b, 5)
+
+
+@pytest.mark.parametrize("failure", ["invalid", "unsupported", "overflow", "native"])
+def test_failed_refit_preserves_fitted_state(failure, monkeypatch):
+    """A refit that fails leaves every fitted attribute as it was (the reference's
+    python/tests/test_hdbscan.py:585-637)."""
+    import cuscan_gb300.hdbscan as hmod
+    x = load_case("blobs_d2")["input"]
+    model = cg.HDBSCAN(min_cluster_size=5, min_samples=5).fit(x)
+    names = ("labels_", "probabilities_", "condensed_tree_", "single_linkage_tree_",
+             "minimum_spanning_tree_", "core_distances_")
+    before = {name: np.array(getattr(model, name), copy=True) for name in names}
+    cut_before = model.dbscan_clustering(0.2).copy()
+    refit = x
+    if failure == "invalid":
+        model.min_cluster_size = 0
+        error = ValueError
+    elif failure == "unsupported":
+        model.metric = "manhattan"
+        error = NotImplementedError
+    elif failure == "overflow":
+        refit = np.array([[1e100, 0.0], [0.0, 0.0]])
+        error = ValueError
+    else:
+        def injected(*args, **kwargs):
+            raise RuntimeError("injected fit-core failure")
+        monkeypatch.setattr(hmod, "fit_hdbscan", injected)
+        error = RuntimeError
+    with pytest.raises(error):
+        model.fit(refit)
+    for name, value in before.items():
+        np.testing.assert_array_equal(getattr(model, name), value)
+    np.testing.assert_array_equal(model.dbscan_clustering(0.2), cut_before)
+
+
+def test_reused_context_buffers_carry_no_state_between_fits():
+    """A context keeps its device buffers between fits. Per-fit state in them (row lower
+    bounds and component bounds of the Borůvka screens, the fp16 operand scale, split-kNN
+    partials) must not leak from one point set into the next: fits of new data of the same
+    size on a used context equal the same fits on a fresh context, bit for bit."""
+    first = synthetic.vmf_like(n=30000, d=128, clusters=40, seed=41)
+    blobs = synthetic.gaussian_mixture(30000, 128, 25, seed=42)
+    vmf = synthetic.vmf_like(n=30000, d=128, clusters=25, seed=43)
+    used = _lib.Context(0)
+    try:
+        used.fit_core(first, 15, _lib.PRECISION_BF16_REFINED)
+        got = [used.fit_core(blobs, 5, _lib.PRECISION_FP16_REFINED),
+               used.fit_core(vmf, 15, _lib.PRECISION_BF16_REFINED),
+               used.fit_core(blobs, 5, _lib.PRECISION_BF16_REFINED)]
+    finally:
+        used.close()
+    cases = [(blobs, 5, _lib.PRECISION_FP16_REFINED), (vmf, 15, _lib.PRECISION_BF16_REFINED),
+             (blobs, 5, _lib.PRECISION_BF16_REFINED)]
+    for (x, ms, prec), a in zip(cases, got):
+        fresh = _lib.Context(0)
+        try:
+            b = fresh.fit_core(x, ms, prec)
+        finally:
+            fresh.close()
+        for key in ("knn_ids", "src", "dst"):
+            np.testing.assert_array_equal(a[key], b[key])
+        for key in ("knn_sq", "core_sq", "wsq"):
+            np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
+        assert a["stats"]["mst_weight"] == b["stats"]["mst_weight"]
