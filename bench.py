@@ -148,9 +148,9 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each screen kernel, from the one-pass ncu capture
 # summarised in profiles/screen_dram_vmf500k_d128.md: the kNN sweep (one launch per fit) and
 # the mean over the Borůvka screen launches of one fit.
-NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_sweep": 138863933184.0,
+NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_screen": 138863933184.0,
                                               "boruvka_candidates": 792814272.0}}
-NCU_TRAFFIC_SCOPE = {"knn_sweep": "ncu dram read+write bytes of the kNN screen launch",
+NCU_TRAFFIC_SCOPE = {"knn_screen": "ncu dram read+write bytes of the kNN screen launch",
                      "boruvka_candidates": "ncu dram read+write bytes, mean per Borůvka screen "
                                            "launch"}
 
@@ -597,6 +597,7 @@ def run_ours(args):
     torch.cuda.synchronize()
 
     step_ms = []
+    screen_ms = []  # the kNN screen launch of every timed step
     stats = None
     launches0 = _lib.launch_count()
     barrier()
@@ -612,6 +613,7 @@ def run_ours(args):
             e1.synchronize()
             step_ms.append(e0.elapsed_time(e1))
             stats = st.as_dict()
+            screen_ms.append(stats["knn_screen_ms"])
             assert m == n - 1
         barrier()
     launches = _lib.launch_count() - launches0
@@ -667,7 +669,12 @@ def run_ours(args):
     w_knn, w_cand = algorithmic_flops(n, d, stats["cross_pairs"])
     t_knn = stats["knn_kernel_ms"] / 1e3
     t_cand = stats["candidate_kernel_ms"] / 1e3
-    if t_knn >= t_cand:
+    if stats["knn_screen_ms"] > 0:
+        # the refined forms: the kNN screen launch, the largest kernel of the fit by device
+        # time (ncu launch list), timed alone with CUDA events on the fit's stream
+        dom, t_dom, w_dom = "knn_screen", float(np.mean(screen_ms)) / 1e3, w_knn
+        achieved = w_dom / t_dom / 1e12
+    elif t_knn >= t_cand:
         dom, achieved, t_dom, w_dom = "knn_sweep", w_knn / t_knn / 1e12, t_knn, w_knn
     else:
         dom = "boruvka_candidates"
@@ -675,7 +682,8 @@ def run_ours(args):
     roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": bf16_peak,
             "unit": "TFLOP/s", "frac": achieved / bf16_peak, "peak_source": f"{peak_src} bf16",
             "traffic": ncu_traffic(args.workload, args.precision, args.n, dom),
-            "kernel_ms": t_dom * 1e3, "algorithmic_tflop": w_dom / 1e12}
+            "kernel_ms": t_dom * 1e3, "algorithmic_tflop": w_dom / 1e12,
+            "knn_stage_ms": stats["knn_kernel_ms"]}
     if roof["traffic"] is not None:
         roof["traffic_scope"] = NCU_TRAFFIC_SCOPE[dom]
     if args.precision != "fp32":
@@ -685,11 +693,11 @@ def run_ours(args):
         roof["tensor_tflop_executed"] = tiles * 2.0 * 128 * 256 * d_pad / 1e12
         roof["executed_frac_fit"] = (roof["tensor_tflop_executed"] * 1e12 / (t_knn + t_cand)
                                      / 1e12 / bf16_peak)
-        roof["work_note"] = ("achieved counts the algorithmic work (every ordered cross pair, "
-                             "no credit for the symmetric screen or for rows that skip a round); "
-                             "tensor_tflop_executed is what the screens ran on the tensor cores "
-                             "over the whole fit, executed_frac_fit that work over the kNN and "
-                             "Borůvka kernel time against the same peak")
+        roof["work_note"] = ("achieved is the named kernel's algorithmic work (the kNN screen: "
+                             "2 d n^2, every ordered pair) over its mean launch time in the timed "
+                             "steps; tensor_tflop_executed is what all screens of one fit ran "
+                             "on the tensor cores, executed_frac_fit that work over the kNN and "
+                             "Borůvka stage time against the same peak")
     if args.precision == "fp32":
         roof["note"] = ("plain form runs f32 direct differences on the SIMT pipes; the fraction "
                         "is against the measured bf16 tensor peak")
@@ -708,6 +716,7 @@ def run_ours(args):
                        stats["components_after_seed"],
                    "core_ms": stats["core_ms"], "mst_ms": stats["mst_ms"],
                    "knn_kernel_ms": stats["knn_kernel_ms"],
+                   "knn_screen_ms": stats["knn_screen_ms"],
                    "candidate_kernel_ms": stats["candidate_kernel_ms"],
                    "knn_fallback_rows": stats["fallback_rows"],
                    "boruvka_fallback_rows": stats["boruvka_fallback_rows"],

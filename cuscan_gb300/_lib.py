@@ -115,6 +115,7 @@ class FitStats(C.Structure):
         ("screen_tile_pairs", C.c_int64),
         ("boruvka_screened_rows", C.c_int64),
         ("mst_weight", C.c_double),
+        ("knn_screen_ms", C.c_double),
     ]
 
     def as_dict(self) -> dict:

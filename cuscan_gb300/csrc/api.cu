@@ -93,6 +93,8 @@ void cuscan_ctx_destroy(cuscan_ctx *ctx) {
         const int count = workspace_buffers(f, all);
         for (int i = 0; i < count; ++i) release(*all[i]);
         f->forest.status = nullptr;
+        for (cudaEvent_t e : f->forest.refined.screen_ev)
+            if (e) cudaEventDestroy(e);
         pack_destroy(f->pack);
         if (f->host_status) cudaFreeHost(f->host_status);
         for (auto &ev : f->ev)
@@ -264,6 +266,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     b.refined.tile_pairs = 0;
     b.refined.screened_rows = 0;
     b.refined.lb_valid = false;
+    b.refined.screen_timed = false;
 
     CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
     CUSCAN_CUDA(ctx, cudaEventRecord(ev[0], s));
@@ -340,6 +343,8 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->screen_tile_pairs = b.refined.tile_pairs;
         stats->boruvka_screened_rows = b.refined.screened_rows;
         stats->mst_weight = hs->mst_weight;
+        stats->knn_screen_ms =
+            b.refined.screen_timed ? elapsed(b.refined.screen_ev[0], b.refined.screen_ev[1]) : 0.0;
     }
     return CUSCAN_OK;
 }

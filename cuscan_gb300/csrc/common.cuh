@@ -24,7 +24,7 @@ struct Buffer {
     size_t bytes = 0;
 };
 
-struct FitWorkspace;  // defined in fit.cu
+struct FitWorkspace;  // defined in workspace.cuh
 
 }  // namespace cuscan
 

@@ -37,6 +37,10 @@ struct RefinedBuffers {
     int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
     int64_t screened_rows = 0;  // query rows of the current fit's Borůvka screens
     bool lb_valid = false;      // rowlb holds bounds of the current fit
+    // CUDA events around the kNN list screen's launch (created on first use); screen_timed
+    // says they hold the current fit's launch
+    cudaEvent_t screen_ev[2] = {nullptr, nullptr};
+    bool screen_timed = false;
 };
 
 struct ForestBuffers {

@@ -1694,7 +1694,12 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     // 24 bounds per row half: enough that nearly every row's unseen bound clears its k-th
     // exact distance at k <= 32 for bf16 screens, and each insertion shifts 24 registers
     constexpr int M = KNN_LIST;
+    for (cudaEvent_t &e : R.screen_ev)
+        if (!e) CUSCAN_CUDA(ctx, cudaEventCreate(&e));
+    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[0], s));
     if ((rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
+    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[1], s));
+    R.screen_timed = true;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
     if ((rc = allow_dynamic_smem(ctx, rerank_knn_kernel<M>, rr_smem))) return rc;

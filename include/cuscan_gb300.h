@@ -89,6 +89,8 @@ typedef struct cuscan_fit_stats {
     double mst_weight;       /* total MST weight: sum of sqrt((double) w_sq) over the edges, the
                                 weights finalize_mst forms (mst.rs:501-512), reduced in f64 on
                                 the device in a fixed order */
+    double knn_screen_ms;    /* the kNN tensor-core screen launch alone (0 when the fit ran
+                                the exact kernels only) */
 } cuscan_fit_stats;
 
 /* ---- context ---- */
