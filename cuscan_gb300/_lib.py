@@ -124,6 +124,7 @@ class FitStats(C.Structure):
 
 PACK_MAX_FITS = 16
 PACK_MAX_ROWS = 2047
+PACK_MAX_FEATURES = 256
 
 
 class FitItem(C.Structure):

@@ -250,8 +250,9 @@ int validate(cuscan_ctx *ctx, const cuscan_fit_item &it, int i) {
         return fail(ctx, CUSCAN_INVALID_INPUT,
                     "fit %d: a packed fit needs 2 to %d rows, got %lld", i, CUSCAN_PACK_MAX_ROWS,
                     (long long)it.n);
-    if (it.d <= 0 || it.d > 256)
-        return fail(ctx, CUSCAN_INVALID_INPUT, "fit %d: a packed fit needs 1 to 256 features", i);
+    if (it.d <= 0 || it.d > CUSCAN_PACK_MAX_FEATURES)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "fit %d: a packed fit needs 1 to %d features", i,
+                    CUSCAN_PACK_MAX_FEATURES);
     if (it.precision != CUSCAN_PRECISION_PLAIN && it.precision != CUSCAN_PRECISION_BF16_REFINED &&
         it.precision != CUSCAN_PRECISION_FP16_REFINED)
         return fail(ctx, CUSCAN_INVALID_CONFIG, "fit %d: unknown precision %d", i, it.precision);

@@ -352,8 +352,11 @@ struct cuscan_server {
         return total;
     }
 
+    // a fit the packed path accepts (a request outside its limits runs on its own, so that it
+    // fails or succeeds exactly as alone and never takes a pack's other fits with it)
     static bool small_fit(const Request *r) {
-        return r->kind == Kind::Fit && r->n <= CUSCAN_PACK_MAX_ROWS;
+        return r->kind == Kind::Fit && r->n <= CUSCAN_PACK_MAX_ROWS &&
+               r->d <= CUSCAN_PACK_MAX_FEATURES;
     }
 
     // Admit queued requests onto idle slots while the budget allows (called with mu held).

@@ -210,10 +210,11 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
  */
 #define CUSCAN_PACK_MAX_FITS 16
 #define CUSCAN_PACK_MAX_ROWS 2047
+#define CUSCAN_PACK_MAX_FEATURES 256
 typedef struct cuscan_fit_item {
     const float *data;      /* host, n x d row-major, finite */
     int64_t n;              /* 2 .. CUSCAN_PACK_MAX_ROWS */
-    int32_t d;              /* 1 .. 256 */
+    int32_t d;              /* 1 .. CUSCAN_PACK_MAX_FEATURES */
     int32_t min_samples;
     int32_t precision;      /* a cuscan_precision */
     int32_t status;         /* out: cuscan_status of this fit */

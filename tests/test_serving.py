@@ -128,6 +128,17 @@ def test_small_fits_behind_a_small_head_run_as_one_pack():
     assert len({infos[r]["slot"] for r in ids[:8]}) == 1
 
 
+def test_fits_outside_the_packed_limits_run_on_their_own():
+    with FitServer(slots=1, budget_bytes=1 << 34, pack_limit=8,
+                   simulated_us_per_kpoint=2000.0) as srv:
+        blocker = srv.submit(np.zeros((20000, 8), np.float32))
+        wide = _lib.PACK_MAX_FEATURES + 1
+        shapes = [(1000, 8), (1000, wide), (1000, 8), (1000, 8)]
+        ids = [srv.submit(np.zeros(s, np.float32)) for s in shapes]
+        infos = drain(srv, [blocker] + ids)
+    assert [infos[r]["pack_size"] for r in ids] == [1, 1, 2, 2]
+
+
 def test_pack_stays_within_the_budget():
     small = bound(2000, 64)
     budget = 3 * small + (1 << 20)
