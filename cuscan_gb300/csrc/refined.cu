@@ -99,7 +99,7 @@ constexpr double SYM_UNBOUNDED_MAX = 0.25;  // largest share of unbounded rows f
 constexpr int64_t SYM_MIN_ROWS = 131072;     // smallest point set for the symmetric screen
 constexpr double SYM_ACTIVE_MIN = 0.9;  // smallest share of screened rows for the symmetric screen
 constexpr int KNN_CAP = 512;  // threshold-mode candidate slots per row half
-constexpr int KNN_LIST = 24;  // kNN list entries per row half
+constexpr int KNN_LIST = 22;  // kNN list entries per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
 
 // ---- PTX wrappers ----
@@ -1691,8 +1691,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     const int32_t *perm = as<int32_t>(b.perm);
     // 3. screen + exact re-rank in sorted positions, outputs in original rows
     if ((rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s))) return rc;
-    // 24 bounds per row half: enough that nearly every row's unseen bound clears its k-th
-    // exact distance at k <= 32 for bf16 screens, and each insertion shifts 24 registers
+    // 22 bounds per row half: enough that nearly every row's unseen bound clears its k-th
+    // exact distance at k <= 32 for bf16 screens (the rest go to the threshold re-screen), and
+    // each insertion shifts 22 registers; 20 and 24 entries measured slower
     constexpr int M = KNN_LIST;
     for (cudaEvent_t &e : R.screen_ev)
         if (!e) CUSCAN_CUDA(ctx, cudaEventCreate(&e));
