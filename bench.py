@@ -148,8 +148,8 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each screen kernel, from the one-pass ncu capture
 # summarised in profiles/screen_dram_vmf500k_d128.md: the kNN sweep (one launch per fit) and
 # the mean over the Borůvka screen launches of one fit.
-NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_screen": 138863933184.0,
-                                              "boruvka_candidates": 792814272.0}}
+NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_screen": 123511651584.0,
+                                              "boruvka_candidates": 773395264.0}}
 NCU_TRAFFIC_SCOPE = {"knn_screen": "ncu dram read+write bytes of the kNN screen launch",
                      "boruvka_candidates": "ncu dram read+write bytes, mean per Borůvka screen "
                                            "launch"}
