@@ -107,20 +107,40 @@ int status_to_error(cuscan_ctx *ctx, int kind, int item) {
     }
 }
 
+void destroy_branch(PackBranch *b) {
+    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->join) cudaEventDestroy(b->join);
+    for (auto &e : b->ev)
+        if (e) cudaEventDestroy(e);
+    delete b;
+}
+
+// Streams and events are created whole or not at all: a workspace or branch is kept only once
+// every handle it needs exists.
 int make_workspace(cuscan_ctx *ctx, int count) {
     FitWorkspace *f = ctx->fit;
     if (!f->pack) {
-        f->pack = new PackWorkspace();
-        CUSCAN_CUDA(ctx, cudaStreamCreateWithFlags(&f->pack->body, cudaStreamNonBlocking));
-        CUSCAN_CUDA(ctx, cudaEventCreateWithFlags(&f->pack->fork, cudaEventDisableTiming));
+        PackWorkspace *p = new PackWorkspace();
+        cudaError_t e = cudaStreamCreateWithFlags(&p->body, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            pack_destroy(p);
+            return cuda_fail(ctx, e, "pack streams");
+        }
+        f->pack = p;
     }
     PackWorkspace &P = *f->pack;
     while ((int)P.branches.size() < count) {
         PackBranch *b = new PackBranch();
+        cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+        for (auto &ev : b->ev)
+            if (e == cudaSuccess) e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) {
+            destroy_branch(b);
+            return cuda_fail(ctx, e, "pack branch streams");
+        }
         P.branches.push_back(b);
-        CUSCAN_CUDA(ctx, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-        CUSCAN_CUDA(ctx, cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
-        for (auto &e : b->ev) CUSCAN_CUDA(ctx, cudaEventCreate(&e));
     }
     return CUSCAN_OK;
 }
@@ -297,13 +317,7 @@ void pack_release(PackWorkspace *p) {
 void pack_destroy(PackWorkspace *p) {
     if (!p) return;
     pack_release(p);
-    for (PackBranch *b : p->branches) {
-        if (b->stream) cudaStreamDestroy(b->stream);
-        if (b->join) cudaEventDestroy(b->join);
-        for (auto &e : b->ev)
-            if (e) cudaEventDestroy(e);
-        delete b;
-    }
+    for (PackBranch *b : p->branches) destroy_branch(b);
     if (p->body) cudaStreamDestroy(p->body);
     if (p->fork) cudaEventDestroy(p->fork);
     delete p;
