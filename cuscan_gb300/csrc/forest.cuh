@@ -34,6 +34,7 @@ struct RefinedBuffers {
     bool fp16 = false;       // in use (the data's range allows a scale)
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;
+    bool range_ok = true;    // the current fit's values keep every screen quantity finite
     int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
     int64_t screened_rows = 0;  // query rows of the current fit's Borůvka screens
     bool lb_valid = false;      // rowlb holds bounds of the current fit

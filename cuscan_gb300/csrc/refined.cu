@@ -1523,26 +1523,36 @@ static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float
 
 // Operand format of this fit's screens: fp16 of x * scale when the caller asked for it and the
 // data's range admits a power-of-two scale, else bf16. One reduction and one host read per fit.
+// Largest d * max|x|^2 for which the screens stay exact: squared norms, dot products, bounds
+// and every exact squared distance (at most 4 d max|x|^2) then stay below FLT_MAX / 4. Above it
+// an f32 quantity may overflow: a bound may become NaN, and exact weights may tie at +inf,
+// where the reference breaks the ties among ALL overflowing pairs, which bounds cannot narrow.
+constexpr double kScreenRangeMax = 3.4028234663852886e38 / 16.0;
+
+// Per fit: the largest |x| (one reduction and one host read) decides whether the screens may run
+// (range_ok) and, when fp16 operands are wanted, their power-of-two scale.
 static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, int64_t n, int d,
                            cudaStream_t s) {
     if (R.have_scale) return CUSCAN_OK;
     R.fp16 = false;
     R.scale = 1.0f;
+    R.range_ok = true;
+    int rc = ensure(ctx, R.absmax, 16, "range reduction");
+    if (rc) return rc;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.absmax.ptr, 0, sizeof(unsigned int), s));
+    const int64_t count = n * (int64_t)d;
+    int64_t blocks = ceil_div(count, 256);
+    if (blocks > 8 * (int64_t)ctx->sm_count) blocks = 8 * (int64_t)ctx->sm_count;
+    CUSCAN_KERNEL(absmax_kernel, (unsigned)blocks, 256, 0, s, x, count,
+                  as<unsigned int>(R.absmax));
+    CUSCAN_LAUNCH(ctx, "absmax_kernel");
+    unsigned int bits = 0;
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(&bits, R.absmax.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    float amax;
+    memcpy(&amax, &bits, sizeof(amax));
+    R.range_ok = std::isfinite(amax) && (double)d * (double)amax * (double)amax <= kScreenRangeMax;
     if (R.want_fp16) {
-        int rc = ensure(ctx, R.absmax, 16, "range reduction");
-        if (rc) return rc;
-        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.absmax.ptr, 0, sizeof(unsigned int), s));
-        const int64_t count = n * (int64_t)d;
-        int64_t blocks = ceil_div(count, 256);
-        if (blocks > 8 * (int64_t)ctx->sm_count) blocks = 8 * (int64_t)ctx->sm_count;
-        CUSCAN_KERNEL(absmax_kernel, (unsigned)blocks, 256, 0, s, x, count,
-                      as<unsigned int>(R.absmax));
-        CUSCAN_LAUNCH(ctx, "absmax_kernel");
-        unsigned int bits = 0;
-        CUSCAN_CUDA(ctx, cudaMemcpyAsync(&bits, R.absmax.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s));
-        CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
-        float amax;
-        memcpy(&amax, &bits, sizeof(amax));
         const float sc = fp16_scale(amax);
         if (sc > 0.0f) {
             R.fp16 = true;
@@ -1671,6 +1681,9 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     refined_layout(n, d, L);
     int rc = choose_operands(ctx, R, x, n, d, s);
     if (rc) return rc;
+    if (!R.range_ok)  // values large enough to overflow f32: the exact sweep decides alone
+        return launch_exact_knn_fp32(ctx, x, n, x, n, d, k, 1, 0, 1, ids, dist, s, b.knn_ids_tmp,
+                                     b.knn_dist_tmp);
     // 1. cells: nearest of npiv evenly spaced pivot rows (exact f32, k = 1)
     const int npiv = (int)(n / 256 < 256 ? (n / 256 < 1 ? 1 : n / 256) : 256);
     rc = ensure(ctx, R.pivots, sizeof(float) * npiv * d, "cell pivots");
@@ -1781,7 +1794,10 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     Layout L;
     refined_layout(n, d, L);
     int rc = choose_operands(ctx, R, xp, n, d, s);
-    if (!rc) rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
+    if (rc) return rc;
+    if (!R.range_ok)  // values large enough to overflow f32: the exact round decides alone
+        return launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s);
+    rc = launch_tile_ranges(ctx, labp, n, clo, chi, s);
     if (!rc) rc = prep(ctx, R, L, xp, n, d, clo, chi, s);
     if (rc) return rc;
     // component bounds: +inf, then the exact cross-component edges of the kNN rows

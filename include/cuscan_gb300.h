@@ -60,7 +60,8 @@ typedef enum cuscan_status {
  * direct differences; FP16_REFINED does the same with fp16 operands of x * 2^k (k chosen from
  * the data's largest |x|), whose 8x smaller rounding error leaves fewer pairs to re-evaluate on
  * data whose norms are large against the neighbour distances (falls back to bf16 operands when
- * no such scale exists). */
+ * no such scale exists). Both refined forms run the exact kernels for data whose values could
+ * overflow an f32 squared norm or distance (d * max|x|^2 > FLT_MAX / 16). */
 typedef enum cuscan_precision {
     CUSCAN_PRECISION_PLAIN = 0,
     CUSCAN_PRECISION_BF16_REFINED = 1,

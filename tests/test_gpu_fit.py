@@ -309,3 +309,37 @@ def test_reused_context_buffers_carry_no_state_between_fits():
         for key in ("knn_sq", "core_sq", "wsq"):
             np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
         assert a["stats"]["mst_weight"] == b["stats"]["mst_weight"]
+
+
+def refined_edge_sets():
+    """Point sets that reach the tensor-core screens (n >= 2048) with the cases the reference's
+    tie and padding rules decide: exact duplicate rows, integer lattices (massive distance ties
+    across tiles), feature counts that are not multiples of the 64-feature K block, ragged last
+    tiles, min_samples of 1 and above the list capacity, and magnitudes at the ends of the fp16
+    operand scale."""
+    rng = np.random.default_rng(2048)
+    base = rng.normal(size=(1200, 24)).astype(np.float32)
+    yield "duplicates", np.concatenate([base, base, base[:700]]), 5
+    yield "lattice_d3", rng.integers(0, 12, size=(4000, 3)).astype(np.float32), 6
+    yield "lattice_d70", rng.integers(0, 3, size=(2500, 70)).astype(np.float32), 4
+    yield "odd_d100", synthetic.blobs_with_noise(n=3001, d=100, centers=9, seed=8), 7
+    yield "ms1", synthetic.blobs_with_noise(n=2600, d=16, centers=5, seed=9), 1
+    yield "ms40", synthetic.blobs_with_noise(n=2600, d=32, centers=5, seed=10), 40
+    yield "tiny", (synthetic.blobs_with_noise(n=3000, d=20, seed=11) * np.float32(1e-30)), 5
+    # just inside the screens' range (d max|x|^2 about FLT_MAX / 64): the screens run
+    big = synthetic.blobs_with_noise(n=3000, d=20, seed=13)
+    yield "large", big * np.float32(np.sqrt(3.4e38 / 64 / 20) / np.abs(big).max()), 5
+    # squared norms and distances overflow f32: exact weights tie at +inf, so the refined
+    # forms hand the fit to the exact kernels
+    yield "huge", (synthetic.blobs_with_noise(n=3000, d=20, seed=12) * np.float32(1e18)), 5
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name,x,ms", list(refined_edge_sets()),
+                         ids=lambda v: v if isinstance(v, str) else "")
+def test_refined_edge_cases_match_oracle(gpu_ctx, name, x, ms, precision):
+    got = gpu_ctx.fit_core(x, ms, precision)
+    assert_fit_equal(got, O.fit_core(x, ms))
+    if precision != _lib.PRECISION_PLAIN:
+        on_screens = name not in ("huge", "ms40")  # ms40: k above the screens' list capacity
+        assert (got["stats"]["refined_rows"] > 0) == on_screens
