@@ -326,6 +326,12 @@ def refined_edge_sets():
     yield "ms1", synthetic.blobs_with_noise(n=2600, d=16, centers=5, seed=9), 1
     yield "ms40", synthetic.blobs_with_noise(n=2600, d=32, centers=5, seed=10), 40
     yield "tiny", (synthetic.blobs_with_noise(n=3000, d=20, seed=11) * np.float32(1e-30)), 5
+    yield "identical", np.ones((2500, 12), np.float32), 5
+    two = np.zeros((3000, 8), np.float32)
+    two[1::2] = 3.0
+    yield "two_points", two, 7
+    yield "line_d1", np.arange(3000, dtype=np.float32)[:, None], 3
+    yield "n2048_ms32", synthetic.vmf_like(n=2048, d=128, clusters=8, seed=14), 32
     # just inside the screens' range (d max|x|^2 about FLT_MAX / 64): the screens run
     big = synthetic.blobs_with_noise(n=3000, d=20, seed=13)
     yield "large", big * np.float32(np.sqrt(3.4e38 / 64 / 20) / np.abs(big).max()), 5
