@@ -116,6 +116,7 @@ class FitStats(C.Structure):
         ("boruvka_screened_rows", C.c_int64),
         ("mst_weight", C.c_double),
         ("knn_screen_ms", C.c_double),
+        ("symmetric_rounds", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

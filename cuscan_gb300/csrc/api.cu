@@ -265,6 +265,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     b.refined.have_scale = false;
     b.refined.tile_pairs = 0;
     b.refined.screened_rows = 0;
+    b.refined.symmetric_rounds = 0;
     b.refined.lb_valid = false;
     b.refined.screen_timed = false;
 
@@ -342,6 +343,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->rescreened_rows = rescreened_rows;
         stats->screen_tile_pairs = b.refined.tile_pairs;
         stats->boruvka_screened_rows = b.refined.screened_rows;
+        stats->symmetric_rounds = b.refined.symmetric_rounds;
         stats->mst_weight = hs->mst_weight;
         stats->knn_screen_ms =
             b.refined.screen_timed ? elapsed(b.refined.screen_ev[0], b.refined.screen_ev[1]) : 0.0;

@@ -37,6 +37,7 @@ struct RefinedBuffers {
     bool range_ok = true;    // the current fit's values keep every screen quantity finite
     int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
     int64_t screened_rows = 0;  // query rows of the current fit's Borůvka screens
+    int64_t symmetric_rounds = 0;  // rounds of the current fit the symmetric screen ran
     bool lb_valid = false;      // rowlb holds bounds of the current fit
     // CUDA events around the kNN list screen's launch (created on first use); screen_timed
     // says they hold the current fit's launch

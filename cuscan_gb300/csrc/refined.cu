@@ -1888,6 +1888,7 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
         CUSCAN_LAUNCH(ctx, "update_row_lb_kernel");
     }
     R.screened_rows += nq;
+    if (sym) ++R.symmetric_rounds;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
     const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
     if ((rc = allow_dynamic_smem(ctx, rerank_boruvka_kernel, rr_smem))) return rc;

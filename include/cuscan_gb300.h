@@ -92,6 +92,7 @@ typedef struct cuscan_fit_stats {
                                 the device in a fixed order */
     double knn_screen_ms;    /* the kNN tensor-core screen launch alone (0 when the fit ran
                                 the exact kernels only) */
+    int64_t symmetric_rounds; /* Borůvka rounds screened with each unordered pair once */
 } cuscan_fit_stats;
 
 /* ---- context ---- */

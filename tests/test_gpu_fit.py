@@ -349,3 +349,21 @@ def test_refined_edge_cases_match_oracle(gpu_ctx, name, x, ms, precision):
     if precision != _lib.PRECISION_PLAIN:
         on_screens = name not in ("huge", "ms40")  # ms40: k above the screens' list capacity
         assert (got["stats"]["refined_rows"] > 0) == on_screens
+
+
+def test_symmetric_boruvka_screen_equals_plain(gpu_ctx):
+    """Every point three times (n = 150,000, min_samples 5): each kNN row holds two exact
+    duplicates and three points of other groups, so every component has a bound from a
+    crossing kNN edge and every row's core is below it. The first round screens every row with
+    the symmetric screen (each unordered pair once, column-side appends). Both refined forms
+    equal the plain form bit for bit."""
+    rng = np.random.default_rng(3)
+    x = np.repeat(rng.random((50000, 8), dtype=np.float32), 3, axis=0)
+    a = gpu_ctx.fit_core(x, 5, _lib.PRECISION_PLAIN)
+    for precision in (_lib.PRECISION_BF16_REFINED, _lib.PRECISION_FP16_REFINED):
+        b = gpu_ctx.fit_core(x, 5, precision)
+        assert b["stats"]["symmetric_rounds"] >= 1, "no round ran the symmetric screen"
+        for key in ("knn_ids", "src", "dst"):
+            np.testing.assert_array_equal(a[key], b[key])
+        for key in ("knn_sq", "core_sq", "wsq"):
+            np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
