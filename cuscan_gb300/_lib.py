@@ -349,16 +349,33 @@ class Context:
         self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out, stream))
 
     # ---- host-pointer fit ----
-    def fit_core(self, x: np.ndarray, min_samples: int, precision: int = PRECISION_PLAIN):
+    @staticmethod
+    def fit_core_outputs(n: int, min_samples: int, empty=np.empty) -> dict:
+        """Output arrays of fit_core for n rows; `empty(shape, dtype)` allocates each (for
+        example from pinned host memory, so that the device-to-host copies run at full speed)."""
+        k = min(int(min_samples), n - 1)
+        m = max(n - 1, 1)
+        return {"knn_ids": empty((n, k), np.int32), "knn_sq": empty((n, k), np.float32),
+                "core_sq": empty((n,), np.float32), "src": empty((m,), np.uint32),
+                "dst": empty((m,), np.uint32), "wsq": empty((m,), np.float32)}
+
+    def fit_core(self, x: np.ndarray, min_samples: int, precision: int = PRECISION_PLAIN,
+                 out: dict | None = None):
+        """Host-pointer fit core. `out` (from fit_core_outputs) receives the results in place;
+        by default new arrays are allocated."""
         x = np.ascontiguousarray(x, dtype=np.float32)
         n, d = x.shape
+        o = out if out is not None else self.fit_core_outputs(n, min_samples)
+        ids, ksq, core = o["knn_ids"], o["knn_sq"], o["core_sq"]
+        src, dst, w = o["src"], o["dst"], o["wsq"]
         k = min(int(min_samples), n - 1)
-        ids = np.empty((n, k), np.int32)
-        ksq = np.empty((n, k), np.float32)
-        core = np.empty(n, np.float32)
-        src = np.empty(max(n - 1, 1), np.uint32)
-        dst = np.empty(max(n - 1, 1), np.uint32)
-        w = np.empty(max(n - 1, 1), np.float32)
+        need = max(n - 1, 1)
+        for a, dt, size in ((ids, np.int32, n * k), (ksq, np.float32, n * k),
+                            (core, np.float32, n), (src, np.uint32, need),
+                            (dst, np.uint32, need), (w, np.float32, need)):
+            if a.dtype != dt or not a.flags.c_contiguous or a.size < size:
+                raise ValueError("fit_core outputs must be C-contiguous arrays of the documented "
+                                 "dtypes and sizes")
         m = C.c_int64(0)
         stats = FitStats()
         self.check(self._lib.cuscan_fit_core(

@@ -367,3 +367,19 @@ def test_symmetric_boruvka_screen_equals_plain(gpu_ctx):
             np.testing.assert_array_equal(a[key], b[key])
         for key in ("knn_sq", "core_sq", "wsq"):
             np.testing.assert_array_equal(bits(a[key]), bits(b[key]))
+
+
+def test_fit_core_into_caller_outputs(gpu_ctx):
+    """fit_core writes into caller-allocated outputs (pinned memory in the bench) exactly what it
+    returns in fresh arrays, and rejects arrays too small for the fit."""
+    x = synthetic.blobs_with_noise(n=3000, d=16, seed=21)
+    fresh = gpu_ctx.fit_core(x, 5, _lib.PRECISION_BF16_REFINED)
+    out = gpu_ctx.fit_core_outputs(3000, 5)
+    got = gpu_ctx.fit_core(x, 5, _lib.PRECISION_BF16_REFINED, out=out)
+    for key in ("knn_ids", "src", "dst"):
+        np.testing.assert_array_equal(got[key], fresh[key])
+    for key in ("knn_sq", "core_sq", "wsq"):
+        np.testing.assert_array_equal(bits(got[key]), bits(fresh[key]))
+    assert got["core_sq"] is out["core_sq"]
+    with pytest.raises(ValueError):
+        gpu_ctx.fit_core(x, 5, out=gpu_ctx.fit_core_outputs(2999, 5))
