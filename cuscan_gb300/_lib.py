@@ -51,6 +51,8 @@ SIGNATURES = {
                                          _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
     "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
+    "cuscan_debug_screen_tile_operands": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32,
+                                                    _VP, C.POINTER(C.c_float), _VP]),
     "cuscan_clusters_from_spanning_tree": (C.c_int, [_U32P, _U32P, _F64P, C.c_int64, _VP,
                                                      C.POINTER(_VP), C.c_char_p, C.c_size_t]),
     "cuscan_clustering_points": (C.c_int64, [_VP]),
@@ -345,8 +347,17 @@ class Context:
                                                     dst, wsq, C.byref(m), C.byref(stats), stream))
         return int(m.value), stats
 
-    def debug_screen_tile(self, data, n, d, tile_out, stream=None):
-        self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out, stream))
+    def debug_screen_tile(self, data, n, d, tile_out, stream=None, operands=None):
+        """Raw accumulator of the first 128 x 256 screen tile; with `operands` (0 bf16, 1 fp16)
+        the chosen format, returning the operand scale (the tile holds scale^2 x the dots)."""
+        if operands is None:
+            self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out,
+                                                          stream))
+            return 1.0
+        scale = C.c_float(0.0)
+        self.check(self._lib.cuscan_debug_screen_tile_operands(
+            self.handle, data, n, d, operands, tile_out, C.byref(scale), stream))
+        return float(scale.value)
 
     # ---- host-pointer fit ----
     @staticmethod

@@ -19,7 +19,7 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                               const float *core, const int32_t *label, cudaStream_t s,
                               int64_t *fallback_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      float *out, cudaStream_t s);
+                      int operands, float *out, float *scale_out, cudaStream_t s);
 size_t refined_workspace_bytes(int64_t n, int d, int k);
 
 // Every device buffer a context holds.
@@ -396,17 +396,25 @@ int cuscan_fit_core(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
     return CUSCAN_OK;
 }
 
-int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
-                             float *tile_out, void *stream) {
+int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                                      int32_t operands, float *tile_out, float *scale_out,
+                                      void *stream) {
     if (!ctx) return CUSCAN_INVALID_INPUT;
     clear_error(ctx);
     if (n < 256 || d <= 0 || !data || !tile_out)
         return fail(ctx, CUSCAN_INVALID_INPUT, "debug tile needs n >= 256 rows");
+    if (operands < 0 || operands > 1)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "unknown operand format");
     CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = pick_stream(ctx, stream);
     int rc = forest_reserve(ctx, ctx->fit->forest, n, d);
     if (rc) return rc;
-    return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, tile_out, s);
+    return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, operands, tile_out, scale_out, s);
+}
+
+int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                             float *tile_out, void *stream) {
+    return cuscan_debug_screen_tile_operands(ctx, data, n, d, 0, tile_out, nullptr, stream);
 }
 
 }  // extern "C"

@@ -243,8 +243,13 @@ __global__ void reduce_tiles_kernel(const float *__restrict__ weights,
     int lane = threadIdx.x & 31;
     if (t >= p) return;
     Fold acc{0xffffffffu, 0x7f800000u, n, n};
-    for (int64_t pos = starts[t] + lane; pos < ends[t]; pos += 32) {
+    // a malformed plan is clamped to the member array [0, n) and to member ids below n, so
+    // it never reads outside the caller's buffers (a valid plan is unaffected)
+    const int64_t lo = starts[t] > 0 ? starts[t] : 0;
+    const int64_t hi = (int64_t)ends[t] < (int64_t)n ? (int64_t)ends[t] : (int64_t)n;
+    for (int64_t pos = lo + lane; pos < hi; pos += 32) {
         uint32_t member = (uint32_t)members[pos];
+        if (member >= n) continue;
         uint32_t original = __float_as_uint(weights[member]);
         int32_t destination = indices[member];
         Fold v{0xffffffffu, 0x7f800000u, n, n};
@@ -265,13 +270,17 @@ __global__ void reduce_tiles_kernel(const float *__restrict__ weights,
 __global__ void reduce_components_kernel(const float *__restrict__ weights,
                                          const int32_t *__restrict__ indices,
                                          const int32_t *__restrict__ partial_offsets,
-                                         const Fold *__restrict__ partial, int64_t c, uint32_t n,
-                                         float *__restrict__ win_w, int32_t *__restrict__ win_meta) {
+                                         const Fold *__restrict__ partial, int64_t c, int64_t p,
+                                         uint32_t n, float *__restrict__ win_w,
+                                         int32_t *__restrict__ win_meta) {
     int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
     int lane = threadIdx.x & 31;
     if (s >= c) return;
     Fold acc{0xffffffffu, 0x7f800000u, n, n};
-    for (int64_t t = partial_offsets[s] + lane; t < partial_offsets[s + 1]; t += 32)
+    // partials of a malformed plan outside [0, p) are not read (a valid plan is unaffected)
+    const int64_t lo = partial_offsets[s] > 0 ? partial_offsets[s] : 0;
+    const int64_t hi = partial_offsets[s + 1] < p ? partial_offsets[s + 1] : p;
+    for (int64_t t = lo + lane; t < hi; t += 32)
         fold_take(acc, partial[t]);
     acc = warp_fold(acc);
     if (lane != 0) return;
@@ -364,7 +373,7 @@ int launch_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t
         CUSCAN_LAUNCH(ctx, "reduce_tiles_kernel");
     }
     CUSCAN_KERNEL(reduce_components_kernel, (unsigned)ceil_div(c * 32, 256), 256, 0, s, 
-        weights, indices, partial_offsets, as<Fold>(scratch), c, (uint32_t)n, win_w, win_meta);
+        weights, indices, partial_offsets, as<Fold>(scratch), c, p, (uint32_t)n, win_w, win_meta);
     CUSCAN_LAUNCH(ctx, "reduce_components_kernel");
     return CUSCAN_OK;
 }
@@ -454,7 +463,7 @@ extern "C" int cuscan_component_reduce_noalloc(
                       indices, members, tile_starts, tile_ends, p, (uint32_t)n, scratch);
     }
     CUSCAN_KERNEL(reduce_components_kernel, (unsigned)ceil_div(c * 32, 256), 256, 0, s, weights,
-                  indices, partial_offsets, scratch, c, (uint32_t)n, win_weights, win_meta);
+                  indices, partial_offsets, scratch, c, p, (uint32_t)n, win_weights, win_meta);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_err(err, err_len, cudaGetErrorString(e));

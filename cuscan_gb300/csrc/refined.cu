@@ -1910,15 +1910,25 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
 }
 
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      float *out, cudaStream_t s) {
+                      int operands, float *out, float *scale_out, cudaStream_t s) {
     Layout L;
     if (!refined_layout(n, d, L))
         return fail(ctx, CUSCAN_CAPACITY, "shape outside the tensor-core tiling");
     RefinedBuffers &R = b.refined;
-    R.fp16 = false;  // the raw accumulator of bf16 operands
-    R.scale = 1.0f;
     R.have_scale = false;
-    int rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
+    R.want_fp16 = operands == 1;
+    int rc = CUSCAN_OK;
+    if (operands == 1) {
+        // fp16 of x * scale with the fit's own power-of-two scale
+        if ((rc = choose_operands(ctx, R, x, n, d, s))) return rc;
+        if (!R.fp16) return fail(ctx, CUSCAN_INVALID_INPUT, "no fp16 scale for this data");
+    } else {
+        R.fp16 = false;  // the raw accumulator of bf16 operands
+        R.scale = 1.0f;
+    }
+    if (scale_out) *scale_out = R.scale;
+    R.have_scale = false;
+    rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
     if (!rc) rc = run_screen<32, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
     if (rc) return rc;
     int fallbacks = 0;

@@ -1,5 +1,11 @@
 """sklearn-style ``HDBSCAN`` with the keyword surface of cuscan's Python estimator.
 
+Provenance: the constructor, its attribute assignments, ``_input_array``, ``_positive_integer``,
+``_validate_parameters`` and the unsupported-keyword checks follow python/cuscan/hdbscan.py of
+lega0208/cuscan (MIT licence, Copyright 2026 M.L.) nearly line for line, because
+they are the drop-in surface: the same keywords, defaults, validation order and messages. The
+fit path behind them (the C ABI calls, finite-row handling around them) is this library's own.
+
 Mirrors ``cuscan.HDBSCAN`` (python/cuscan/hdbscan.py:148-574 of lega0208/cuscan): the same
 constructor keywords, validation messages, fitted attributes and error types. The fit core
 (exact kNN core distances + Borůvka MST) runs in the sm_103a library through its C ABI; the

@@ -139,6 +139,9 @@ int cuscan_boruvka_candidates(cuscan_ctx *ctx, const float *data, const float *c
  * win_meta[c*5] = (source, destination, bad_row, error_kind, bad_destination), exactly as
  * HdbscanOps::component_reduce (crates/hdbscan/src/backend.rs:90-98;
  * crates/hdbscan/src/kernels/component_reduce.rs:28-353).
+ * The plan arrays must form a valid plan. A malformed one is not detected, but it cannot make
+ * the kernels read outside the buffers: CSR positions are clamped to [0, n), member ids at or
+ * above n are skipped, and partial offsets are clamped to [0, p).
  */
 int cuscan_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t *indices,
                             const int32_t *members, const int32_t *tile_starts,
@@ -158,6 +161,9 @@ int cuscan_component_reduce(cuscan_ctx *ctx, const float *weights, const int32_t
  *    (cudaGetSymbolAddress); make that first call before any stream capture.
  *  - Every call shares the one array: calls that overlap on the GPU (different streams, or
  *    different host threads on the same device) race and must be serialised by the caller.
+ *  - The address is cached per device for the life of the process: resetting a device
+ *    (cudaDeviceReset, or a reset of its primary context) after the first call is not
+ *    supported, because the module and its array may then live at another address.
  *  - stream is a cudaStream_t as void* (NULL = the legacy default stream); err (may be NULL)
  *    receives the message of a failure.
  */
@@ -239,6 +245,14 @@ int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, int32_t coun
  */
 int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
                              float *tile_out, void *stream);
+/*
+ * The same diagnostic for a chosen operand format: operands 0 = bf16 (as above), 1 = fp16 of
+ * x * scale with the power-of-two scale the fp16-refined fits choose for this data (written to
+ * *scale_out when given; the accumulator is then scale^2 times the dot products).
+ */
+int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
+                                      int32_t operands, float *tile_out, float *scale_out,
+                                      void *stream);
 
 /* ---- host-side extraction (no device work) ---- */
 

@@ -143,6 +143,170 @@ int orc_exact_neighbors(const float *query, int64_t nq, const float *reference, 
 }
 
 /*
+ * Blocked forms of the two all-pairs loops, for checking large fits in reasonable time.
+ * ORC_RB reference rows are copied feature-major into a per-thread block, so that the
+ * sequential fmaf chains of ORC_RB pairs advance together (one vector FMA per feature where
+ * the compiler vectorises). Each pair still evaluates acc = fmaf(q_f - r_f, q_f - r_f, acc) in
+ * feature order from 0, exactly sq_dist, and the candidates of a row are offered in ascending
+ * reference order, so outputs are bit-identical to the row-at-a-time loops
+ * (tests/test_oracle_consistency.py checks this). The row-at-a-time loops remain the timed
+ * CPU baseline: they are the reference's own per-row loop structure.
+ */
+#define ORC_RB 16
+#define ORC_QB 64
+static int g_blocked = 1;
+
+/* 1: orc_fit_core uses the blocked loops (default); 0: the row-at-a-time loops. */
+void orc_set_blocked(int on) { g_blocked = on ? 1 : 0; }
+
+/* Copy reference rows [r0, r0 + nb) feature-major into tb[d][ORC_RB] (zero padded). */
+static void transpose_block(const float *reference, int64_t r0, int nb, int d, float *tb) {
+    for (int j = 0; j < ORC_RB; ++j) {
+        if (j < nb) {
+            const float *src = reference + (r0 + j) * d;
+            for (int f = 0; f < d; ++f) tb[f * ORC_RB + j] = src[f];
+        } else {
+            for (int f = 0; f < d; ++f) tb[f * ORC_RB + j] = 0.0f;
+        }
+    }
+}
+
+/* Sequential-FMA squared distances of one query row to the ORC_RB rows of a block. */
+static inline void block_dists(const float *q, const float *tb, int d, float *acc) {
+    for (int j = 0; j < ORC_RB; ++j) acc[j] = 0.0f;
+    for (int f = 0; f < d; ++f) {
+        const float qf = q[f];
+        const float *t = tb + f * ORC_RB;
+        for (int j = 0; j < ORC_RB; ++j) {
+            const float delta = qf - t[j];
+            acc[j] = fmaf(delta, delta, acc[j]);
+        }
+    }
+}
+
+/* Blocked orc_exact_neighbors: the same slots, ties and padding. */
+int orc_exact_neighbors_blocked(const float *query, int64_t nq, const float *reference,
+                                int64_t nr, int d, int k, int exclude_self, int64_t query_offset,
+                                int squared, int32_t *ids, float *dist) {
+    if (nq < 0 || nr <= 0 || d <= 0 || k <= 0) return ORC_INVALID_INPUT;
+    if (nr > INT32_MAX) return ORC_OVERFLOW;
+    const float pad = squared ? ORC_INF : ORC_FLT_MAX;
+    const int64_t chunks = (nq + ORC_QB - 1) / ORC_QB;
+    int failed = 0;
+#pragma omp parallel num_threads(orc_max_threads())
+    {
+        float *tb = (float *)malloc(sizeof(float) * (size_t)d * ORC_RB);
+        if (!tb) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t ch = 0; ch < chunks; ++ch) {
+            if (!tb) continue;
+            const int64_t q0 = ch * ORC_QB, q1 = q0 + ORC_QB < nq ? q0 + ORC_QB : nq;
+            for (int64_t row = q0; row < q1; ++row)
+                for (int s = 0; s < k; ++s) {
+                    ids[row * k + s] = (int32_t)nr;
+                    dist[row * k + s] = pad;
+                }
+            float acc[ORC_RB];
+            for (int64_t r0 = 0; r0 < nr; r0 += ORC_RB) {
+                const int nb = (int)(nr - r0 < ORC_RB ? nr - r0 : ORC_RB);
+                transpose_block(reference, r0, nb, d, tb);
+                for (int64_t row = q0; row < q1; ++row) {
+                    block_dists(query + row * d, tb, d, acc);
+                    int32_t *id = ids + row * k;
+                    float *ds = dist + row * k;
+                    const int64_t self = query_offset + row;
+                    for (int j = 0; j < nb; ++j) {
+                        const int64_t r = r0 + j;
+                        if (exclude_self && r == self) continue;
+                        const float distance = acc[j];
+                        const int w = k - 1;
+                        if (distance < ds[w] ||
+                            (distance == ds[w] && r < (int64_t)(uint32_t)id[w])) {
+                            int slot = k - 1;
+                            while (slot > 0) {
+                                const int p = slot - 1;
+                                if (distance < ds[p] ||
+                                    (distance == ds[p] && r < (int64_t)(uint32_t)id[p])) {
+                                    id[slot] = id[p];
+                                    ds[slot] = ds[p];
+                                    --slot;
+                                } else {
+                                    break;
+                                }
+                            }
+                            id[slot] = (int32_t)r;
+                            ds[slot] = distance;
+                        }
+                    }
+                }
+            }
+            if (!squared)
+                for (int64_t row = q0; row < q1; ++row)
+                    for (int s = 0; s < k; ++s) dist[row * k + s] = sqrtf(dist[row * k + s]);
+        }
+        free(tb);
+    }
+    return failed ? ORC_MEMORY : ORC_OK;
+}
+
+/* Blocked orc_boruvka_candidates: the same (weight, j) minimum per row. */
+int orc_boruvka_candidates_blocked(const float *x, const float *core_sq,
+                                   const int32_t *components, int64_t n, int d, float *w_out,
+                                   int32_t *dst_out) {
+    if (n <= 0 || d <= 0) return ORC_INVALID_INPUT;
+    const int64_t chunks = (n + ORC_QB - 1) / ORC_QB;
+    int failed = 0;
+#pragma omp parallel num_threads(orc_max_threads())
+    {
+        float *tb = (float *)malloc(sizeof(float) * (size_t)d * ORC_RB);
+        if (!tb) {
+#pragma omp atomic write
+            failed = 1;
+        }
+#pragma omp for schedule(dynamic, 1)
+        for (int64_t ch = 0; ch < chunks; ++ch) {
+            if (!tb) continue;
+            const int64_t q0 = ch * ORC_QB, q1 = q0 + ORC_QB < n ? q0 + ORC_QB : n;
+            for (int64_t i = q0; i < q1; ++i) {
+                w_out[i] = ORC_INF;
+                dst_out[i] = (int32_t)n;
+            }
+            float acc[ORC_RB];
+            for (int64_t r0 = 0; r0 < n; r0 += ORC_RB) {
+                const int nb = (int)(n - r0 < ORC_RB ? n - r0 : ORC_RB);
+                transpose_block(x, r0, nb, d, tb);
+                for (int64_t i = q0; i < q1; ++i) {
+                    const int32_t ci = components[i];
+                    int any = 0;
+                    for (int j = 0; j < nb; ++j) any |= components[r0 + j] != ci;
+                    if (!any) continue;
+                    block_dists(x + i * d, tb, d, acc);
+                    const float core = core_sq[i];
+                    float best = w_out[i];
+                    int64_t best_index = dst_out[i];
+                    for (int j = 0; j < nb; ++j) {
+                        const int64_t r = r0 + j;
+                        if (components[r] == ci) continue;
+                        const float weight = fmaxf(fmaxf(acc[j], core), core_sq[r]);
+                        if (weight < best || (weight == best && r < best_index)) {
+                            best = weight;
+                            best_index = r;
+                        }
+                    }
+                    w_out[i] = best;
+                    dst_out[i] = (int32_t)best_index;
+                }
+            }
+        }
+        free(tb);
+    }
+    return failed ? ORC_MEMORY : ORC_OK;
+}
+
+/*
  * Core distances from a kNN row block (crates/hdbscan/src/estimator.rs:668-676):
  * +inf when min_samples >= n, 0 when min_samples == 1, else column min_samples-1.
  */
@@ -509,7 +673,8 @@ int orc_fit_core(const float *x, int64_t n, int d, int min_samples, int32_t *knn
     if (n <= 1 || d <= 0 || min_samples <= 0) return ORC_INVALID_INPUT;
     if (n > INT32_MAX) return ORC_OVERFLOW;
     int k = (int64_t)min_samples < n - 1 ? min_samples : (int)(n - 1);
-    int rc = orc_exact_neighbors(x, n, x, n, d, k, 1, 0, 1, knn_ids, knn_sq);
+    int rc = g_blocked ? orc_exact_neighbors_blocked(x, n, x, n, d, k, 1, 0, 1, knn_ids, knn_sq)
+                       : orc_exact_neighbors(x, n, x, n, d, k, 1, 0, 1, knn_ids, knn_sq);
     if (rc) return rc;
     orc_core_from_knn(knn_sq, n, k, min_samples, core_sq);
 
@@ -556,7 +721,8 @@ int orc_fit_core(const float *x, int64_t n, int d, int min_samples, int32_t *knn
             stats->round_components[rounds] = c;
             stats->round_cross_pairs[rounds] = (double)n * (double)n - same;
         }
-        rc = orc_boruvka_candidates(x, core_sq, labels, n, d, cw, cd);
+        rc = g_blocked ? orc_boruvka_candidates_blocked(x, core_sq, labels, n, d, cw, cd)
+                       : orc_boruvka_candidates(x, core_sq, labels, n, d, cw, cd);
         if (rc) goto done;
         rc = orc_component_reduce(cw, cd, members, offsets, n, c, ww, wm);
         if (rc) goto done;

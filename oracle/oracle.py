@@ -62,6 +62,9 @@ def lib():
         L.orc_finalize_mst.argtypes = [_U32P, _U32P, _F32P, C.c_int64, _F64P]
         L.orc_pair_distances.argtypes = [_F32P, _F32P, C.c_int64, C.c_int, C.c_int, _F32P]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_blocked.argtypes = [C.c_int]
+        L.orc_exact_neighbors_blocked.argtypes = L.orc_exact_neighbors.argtypes
+        L.orc_boruvka_candidates_blocked.argtypes = L.orc_boruvka_candidates.argtypes
         L.orc_prediction_cores.argtypes = [_F32P, C.c_int64, C.c_int, C.c_int, _F64P]
         L.orc_predict_candidates.argtypes = [_I64P, _I64P, _F32P, _F32P, C.c_int64, _I32P,
                                              C.c_int64, _U32P, C.c_int64, C.c_int, _F64P, _I32P,
@@ -89,15 +92,24 @@ def max_threads() -> int:
     return int(lib().orc_max_threads())
 
 
-def exact_neighbors(query, reference, k, *, exclude_self=True, query_offset=0, squared=True):
+def set_blocked(on: bool) -> None:
+    """Whether fit_core runs the blocked all-pairs loops (the default; bit-identical to the
+    row-at-a-time loops, several times faster where the compiler vectorises them)."""
+    lib().orc_set_blocked(int(bool(on)))
+
+
+def exact_neighbors(query, reference, k, *, exclude_self=True, query_offset=0, squared=True,
+                    blocked=False):
+    """Exact kNN rows; `blocked` selects the blocked loop (same bits), otherwise the
+    row-at-a-time loop that the CPU baseline times."""
     q = np.ascontiguousarray(query, dtype=np.float32)
     r = np.ascontiguousarray(reference, dtype=np.float32)
     nq, d = q.shape
     ids = np.empty((nq, k), np.int32)
     dist = np.empty((nq, k), np.float32)
-    _check(lib().orc_exact_neighbors(_p(q, _F32P), nq, _p(r, _F32P), r.shape[0], d, k,
-                                     int(exclude_self), query_offset, int(squared),
-                                     _p(ids, _I32P), _p(dist, _F32P)), "exact_neighbors")
+    fn = lib().orc_exact_neighbors_blocked if blocked else lib().orc_exact_neighbors
+    _check(fn(_p(q, _F32P), nq, _p(r, _F32P), r.shape[0], d, k, int(exclude_self), query_offset,
+              int(squared), _p(ids, _I32P), _p(dist, _F32P)), "exact_neighbors")
     return ids, dist
 
 
@@ -126,15 +138,16 @@ def init_from_knn(core_sq, neighbors, knn_sq):
     return src[:e].copy(), dst[:e].copy(), w[:e].copy(), labels
 
 
-def boruvka_candidates(x, core_sq, components):
+def boruvka_candidates(x, core_sq, components, *, blocked=False):
     x = np.ascontiguousarray(x, np.float32)
     core_sq = np.ascontiguousarray(core_sq, np.float32)
     components = np.ascontiguousarray(components, np.int32)
     n, d = x.shape
     w = np.empty(n, np.float32)
     dst = np.empty(n, np.int32)
-    _check(lib().orc_boruvka_candidates(_p(x, _F32P), _p(core_sq, _F32P), _p(components, _I32P),
-                                        n, d, _p(w, _F32P), _p(dst, _I32P)), "boruvka_candidates")
+    fn = lib().orc_boruvka_candidates_blocked if blocked else lib().orc_boruvka_candidates
+    _check(fn(_p(x, _F32P), _p(core_sq, _F32P), _p(components, _I32P), n, d, _p(w, _F32P),
+              _p(dst, _I32P)), "boruvka_candidates")
     return w, dst
 
 

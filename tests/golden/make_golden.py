@@ -7,9 +7,9 @@ they are, into one compressed ``{case}.npz`` here plus ``manifest.json``, so tha
 without the reference checkout. It also copies ``hdbscan_prediction.json`` (the
 ``approximate_predict`` fixture generated by the reference from the original ``hdbscan``
 package: controlled trees, fitted models with candidate rows and expected predictions) as it is.
-Run it where the reference is mounted:
+Run it where the reference checkout is available, passing its root directory:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout root>
 """
 from __future__ import annotations
 
@@ -53,4 +53,6 @@ def main(reference_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout root>")
+    main(sys.argv[1])

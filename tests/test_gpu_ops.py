@@ -193,3 +193,34 @@ def test_tensor_core_tile_matches_bf16_products(gpu_ctx, n, d, seed):
     scale = np.abs(xb[:128]) @ np.abs(xb[:cols]).T
     err = np.abs(got[:, :cols] - exp)
     assert np.all(err <= 1e-5 * scale + 1e-30), float(np.max(err / np.maximum(scale, 1e-30)))
+
+
+def test_component_reduce_clamps_a_malformed_plan(gpu_ctx):
+    """Plan arrays that overrun their buffers (partial offsets past p, tile ends past n, member
+    ids >= n) are clamped instead of read out of bounds: the result equals the same call on
+    the clamped plan."""
+    rng = np.random.default_rng(21)
+    n = 3000
+    labels = rng.integers(0, 40, size=n).astype(np.int32)
+    plan = O.component_plan(labels, 64)
+    w = rng.integers(0, 50, size=n).astype(np.float32)
+    dst = rng.integers(0, n, size=n).astype(np.int32)
+    p = plan.tile_starts.shape[0]
+    bad = O.ComponentPlan(plan.members.copy(), plan.offsets, plan.tile_starts.copy(),
+                          plan.tile_ends.copy(), plan.partial_offsets.copy())
+    bad.partial_offsets[-1] = p + 1000          # past the last partial
+    bad.tile_ends[-1] = n + 77                  # past the member array
+    bad.members[5] = n + 9                      # a member id outside the points
+    fixed = O.ComponentPlan(bad.members.copy(), bad.offsets, bad.tile_starts,
+                            np.minimum(bad.tile_ends, n).astype(np.int32),
+                            np.minimum(bad.partial_offsets, p).astype(np.int32))
+    fixed.members[5] = 0
+    w_fixed = w.copy()
+    # member 5's slot now names point 0; give point 0 a weight that cannot win so that skipping
+    # the bad id and reading point 0 give the same reduction
+    w_fixed[0] = np.inf
+    w[0] = np.inf
+    ww_bad, wm_bad = gpu_reduce(gpu_ctx, w, dst, bad, n)
+    ww_fix, wm_fix = gpu_reduce(gpu_ctx, w_fixed, dst, fixed, n)
+    np.testing.assert_array_equal(wm_bad, wm_fix)
+    np.testing.assert_array_equal(bits(ww_bad), bits(ww_fix))
