@@ -107,11 +107,21 @@ def request_points(spec: dict) -> np.ndarray:
     return gaussian_mixture(spec["n"], spec["d"], spec["blobs"], seed=spec["seed"])
 
 
+def repeated_points(n: int = 150_000, d: int = 8, copies: int = 3, seed: int = 3) -> np.ndarray:
+    """n // copies uniform points in [0, 1)^d, each repeated `copies` times in a row: every
+    kNN row holds exact duplicates and points of other groups, the case where a Borůvka round
+    screens nearly every row."""
+    rng = np.random.default_rng(seed)
+    return np.repeat(rng.random((n // copies, d), dtype=np.float32), copies, axis=0)
+
+
 WORKLOADS = {
     # name: (generator, kwargs, min_samples, min_cluster_size)
     "blobs_2k_d10": (blobs_with_noise, dict(n=2000, d=10, seed=42), 5, 5),
     "aniso_100k_d64": (anisotropic_mixture, dict(n=100_000, d=64, seed=43), 10, 50),
     "vmf_500k_d128": (vmf_like, dict(n=500_000, d=128, seed=44), 15, 100),
+    # profiling case of the symmetric Borůvka screen (not a benchmark configuration)
+    "triplicates_150k_d8": (repeated_points, dict(n=150_000, d=8, seed=3), 5, 5),
 }
 
 
