@@ -566,6 +566,33 @@ def serving_section(args) -> dict:
     return out
 
 
+def serving_summary(serving: dict) -> dict:
+    """The compact serving figures, kept in `config` (which survives truncation of the line):
+    per precision the Poisson stream's p50/p99, the p99 of fits with n >= 10,000 and the
+    saturation rate; the mixed stream's fit and predict p99; the packing speed-up."""
+    out = {}
+    for prec, res in serving.items():
+        if not isinstance(res, dict) or "poisson" not in res:
+            continue
+        po = res["poisson"]
+        big = po["by_size"].get("n10000-50000", {})
+        out[prec] = {"p50_ms": round(po["p50_ms"], 2), "p99_ms": round(po["p99_ms"], 2),
+                     "p99_n_ge_10000_ms": round(big.get("p99_ms", float("nan")), 2),
+                     "saturation_req_per_s": round(res["saturation"]["req_per_s"], 1),
+                     "poisson_req_per_s": round(po["req_per_s"], 1)}
+    for prec, res in serving.get("mixed", {}).items():
+        if isinstance(res, dict) and "fit" in res:
+            out[f"mixed_{prec}"] = {
+                "fit_p99_ms": round(res["fit"]["p99_ms"], 2),
+                "predict_p99_ms": round(res.get("predict", {}).get("p99_ms", float("nan")), 2),
+                "req_per_s": round(res["req_per_s"], 1),
+                "predict_mix_equals_alone": res["predict_mix_equals_alone"]}
+    pack = serving.get("small_fit_packing")
+    if pack:
+        out["packing_speedup"] = round(pack["packing_speedup"], 3)
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -685,6 +712,13 @@ def run_ours(args):
             assert m == n - 1
         barrier()
     launches = _lib.launch_count() - launches0
+    # per Borůvka round of the last timed fit: rows screened, tensor-core tiles run and their
+    # share of a dense round's tiles (every query block against every tile)
+    dense_tiles = -(-n // 128) * -(-n // 256)
+    round_detail = [{"rows": r["rows"], "tiles": r["tiles"], "ms": round(r["ms"], 3),
+                     "executed_tile_frac": round(r["tiles"] / dense_tiles, 4),
+                     "cross_pair_frac": round(r["cross_pairs"] / (float(n) * n), 4)}
+                    for r in ctx.round_stats()]
     pts_per_s, worst_s = replicas.aggregate_throughput(n, args.steps, float(np.sum(step_ms)) / 1e3,
                                                        device="cuda")
     ms_per_step = worst_s * 1e3 / args.steps
@@ -792,6 +826,9 @@ def run_ours(args):
                    "rescreened_rows": stats["rescreened_rows"],
                    "boruvka_screened_rows": stats["boruvka_screened_rows"],
                    "mst_weight_f64": stats["mst_weight"],
+                   "operand_format": {-1: "none", 0: "bf16", 1: "fp16", 2: "split bf16"}[
+                       int(stats["operand_format"])],
+                   "boruvka_rounds": round_detail,
                    "algorithmic_tflop_per_step": (w_knn + w_cand) / 1e12},
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_pts_per_s / 1e6, "unit": "Mpts/s",
@@ -801,10 +838,15 @@ def run_ours(args):
     }
     if fp32 is not None:
         line["fp32_plain"] = fp32
+    if fp32 is not None:
+        line["config"]["fp32_plain"] = {k2: fp32[k2] for k2 in (
+            "ms_per_step", f"{args.precision}_speedup", "outputs_bit_identical",
+            "mst_weight_f64_equal")}
     if rank == 0 and world == 1 and not args.no_serve:
         del xd, ids, ksq, core, src, dst, wsq, flush
         torch.cuda.empty_cache()
         line["serving"] = serving_section(args)
+        line["config"]["serving_summary"] = serving_summary(line["serving"])
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k2: v for k2, v in cpu_baseline(
             x, ms, stats["cross_pairs"], args.cpu_seconds).items()

@@ -52,7 +52,16 @@ SIGNATURES = {
     "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_debug_screen_tile_operands": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32,
-                                                    _VP, C.POINTER(C.c_float), _VP]),
+                                                    _VP, _VP, C.POINTER(C.c_float), _VP]),
+    "cuscan_fit_round_stats": (C.c_int, [_VP, C.c_int32, _VP, _VP, _VP, _VP]),
+    "cuscan_shard_seed": (C.c_int, [_VP, C.c_int64, C.c_int32, C.c_int32, _VP, _VP, _VP, _VP,
+                                    _VP, _VP, _VP, C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64), _VP]),
+    "cuscan_shard_round_keys": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int64, C.c_int32, C.c_int64,
+                                          C.c_int64, _VP, _VP]),
+    "cuscan_shard_round_merge": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int64, C.c_int32, _VP, _VP,
+                                           _VP, _VP, C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int64), C.POINTER(C.c_double), _VP]),
     "cuscan_clusters_from_spanning_tree": (C.c_int, [_U32P, _U32P, _F64P, C.c_int64, _VP,
                                                      C.POINTER(_VP), C.c_char_p, C.c_size_t]),
     "cuscan_clustering_points": (C.c_int64, [_VP]),
@@ -119,6 +128,7 @@ class FitStats(C.Structure):
         ("mst_weight", C.c_double),
         ("knn_screen_ms", C.c_double),
         ("symmetric_rounds", C.c_int64),
+        ("operand_format", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -347,17 +357,55 @@ class Context:
                                                     dst, wsq, C.byref(m), C.byref(stats), stream))
         return int(m.value), stats
 
-    def debug_screen_tile(self, data, n, d, tile_out, stream=None, operands=None):
-        """Raw accumulator of the first 128 x 256 screen tile; with `operands` (0 bf16, 1 fp16)
-        the chosen format, returning the operand scale (the tile holds scale^2 x the dots)."""
+    def debug_screen_tile(self, data, n, d, tile_out, stream=None, operands=None, rows_out=None):
+        """Raw accumulator of the first 128 x 256 screen tile; with `operands` (0 bf16, 1 fp16,
+        2 split bf16) the chosen format, returning the operand scale (the tile holds scale^2 x
+        the dots). rows_out (device float[n][4]) receives every row's bound terms
+        (ps, pb, cm, m)."""
         if operands is None:
             self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out,
                                                           stream))
             return 1.0
         scale = C.c_float(0.0)
         self.check(self._lib.cuscan_debug_screen_tile_operands(
-            self.handle, data, n, d, operands, tile_out, C.byref(scale), stream))
+            self.handle, data, n, d, operands, tile_out, rows_out, C.byref(scale), stream))
         return float(scale.value)
+
+    def round_stats(self) -> list[dict]:
+        """Per Borůvka round of this context's last fit: screened rows, tensor-core tiles,
+        candidate-kernel ms and ordered cross-component pairs."""
+        cap = 64
+        rows = np.zeros(cap, np.int64)
+        tiles = np.zeros(cap, np.int64)
+        ms = np.zeros(cap, np.float64)
+        cross = np.zeros(cap, np.float64)
+        count = self._lib.cuscan_fit_round_stats(self.handle, cap, rows.ctypes.data,
+                                                 tiles.ctypes.data, ms.ctypes.data,
+                                                 cross.ctypes.data)
+        return [{"rows": int(rows[r]), "tiles": int(tiles[r]), "ms": float(ms[r]),
+                 "cross_pairs": float(cross[r])} for r in range(min(max(count, 0), cap))]
+
+    # ---- row shards (device pointers) ----
+    def shard_seed(self, n, d, min_samples, knn_ids, knn_sq, core_sq, labels, src, dst, wsq,
+                   stream=None):
+        m, comps = C.c_int64(0), C.c_int64(0)
+        self.check(self._lib.cuscan_shard_seed(self.handle, n, d, min_samples, knn_ids, knn_sq,
+                                               core_sq, labels, src, dst, wsq, C.byref(m),
+                                               C.byref(comps), stream))
+        return int(m.value), int(comps.value)
+
+    def shard_round_keys(self, data, core_sq, labels, n, d, row_begin, row_end, row_keys,
+                         stream=None):
+        self.check(self._lib.cuscan_shard_round_keys(self.handle, data, core_sq, labels, n, d,
+                                                     row_begin, row_end, row_keys, stream))
+
+    def shard_round_merge(self, data, core_sq, labels, n, d, row_keys, src, dst, wsq,
+                          stream=None):
+        m, comps, w = C.c_int64(0), C.c_int64(0), C.c_double(float("nan"))
+        self.check(self._lib.cuscan_shard_round_merge(self.handle, data, core_sq, labels, n, d,
+                                                      row_keys, src, dst, wsq, C.byref(m),
+                                                      C.byref(comps), C.byref(w), stream))
+        return int(m.value), int(comps.value), float(w.value)
 
     # ---- host-pointer fit ----
     @staticmethod

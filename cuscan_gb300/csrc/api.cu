@@ -19,7 +19,9 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                               const float *core, const int32_t *label, cudaStream_t s,
                               int64_t *fallback_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      int operands, float *out, float *scale_out, cudaStream_t s);
+                      int operands, float *out, float *rows_out, float *scale_out,
+                      cudaStream_t s);
+int refined_operand_format(const ForestBuffers &b);
 size_t refined_workspace_bytes(int64_t n, int d, int k);
 
 // Every device buffer a context holds.
@@ -263,6 +265,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     int64_t refined_rows = 0, fallback_rows = 0, boruvka_fallback_rows = 0, rescreened_rows = 0;
     b.refined.want_fp16 = precision == CUSCAN_PRECISION_FP16_REFINED;
     b.refined.have_scale = false;
+    b.refined.split = false;
     b.refined.tile_pairs = 0;
     b.refined.screened_rows = 0;
     b.refined.symmetric_rounds = 0;
@@ -294,7 +297,9 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     int64_t components = (int64_t)hs->components;
     int64_t rounds = 0;
     double cand_ms = 0.0, cross_pairs = 0.0;
+    f->round_count = 0;
     while (components > 1) {
+        const int64_t rows0 = b.refined.screened_rows, tiles0 = b.refined.tile_pairs;
         if (rounds > 64) return fail(ctx, CUSCAN_NUMERICAL, "Boruvka did not converge");
         if ((rc = forest_sort_by_component(ctx, b, data, core_sq, label, n, d, s))) return rc;
         unsigned long long *row_keys = as<unsigned long long>(b.row_keys);
@@ -315,6 +320,13 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if ((rc = read_status(ctx, b.status, hs, s))) return rc;
         cand_ms += elapsed(ev[4], ev[5]);
         cross_pairs += (double)n * (double)n - hs->same_pairs;
+        if (f->round_count < FitWorkspace::kMaxRoundLog) {
+            const int r = f->round_count++;
+            f->round_rows[r] = refined ? b.refined.screened_rows - rows0 : n;
+            f->round_tiles[r] = b.refined.tile_pairs - tiles0;
+            f->round_ms[r] = elapsed(ev[4], ev[5]);
+            f->round_cross[r] = (double)n * (double)n - hs->same_pairs;
+        }
         if (hs->err_kind) return status_error(ctx, hs->err_kind);
         ++rounds;
         components = (int64_t)hs->components;
@@ -347,6 +359,7 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         stats->mst_weight = hs->mst_weight;
         stats->knn_screen_ms =
             b.refined.screen_timed ? elapsed(b.refined.screen_ev[0], b.refined.screen_ev[1]) : 0.0;
+        stats->operand_format = refined ? refined_operand_format(b) : -1;
     }
     return CUSCAN_OK;
 }
@@ -396,25 +409,134 @@ int cuscan_fit_core(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
     return CUSCAN_OK;
 }
 
+int cuscan_fit_round_stats(const cuscan_ctx *ctx, int32_t max_rounds, int64_t *rows,
+                           int64_t *tiles, double *ms, double *cross_pairs) {
+    if (!ctx || !ctx->fit || max_rounds < 0) return -1;
+    const FitWorkspace *f = ctx->fit;
+    const int count = f->round_count < max_rounds ? f->round_count : max_rounds;
+    for (int r = 0; r < count; ++r) {
+        if (rows) rows[r] = f->round_rows[r];
+        if (tiles) tiles[r] = f->round_tiles[r];
+        if (ms) ms[r] = f->round_ms[r];
+        if (cross_pairs) cross_pairs[r] = f->round_cross[r];
+    }
+    return f->round_count;
+}
+
+// ---- row shards: one fit split by query rows over ranks that exchange row keys ----
+int cuscan_shard_seed(cuscan_ctx *ctx, int64_t n, int32_t d, int32_t min_samples,
+                      const int32_t *knn_ids, const float *knn_sq, float *core_sq,
+                      int32_t *labels, uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                      int64_t *n_edges, int64_t *components, void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n < 2 || d <= 0) return fail(ctx, CUSCAN_INVALID_INPUT, "a fit needs at least two rows");
+    if (min_samples <= 0) return fail(ctx, CUSCAN_INVALID_CONFIG, "min_samples must be positive");
+    if (n > INT32_MAX - 1) return fail(ctx, CUSCAN_OVERFLOW, "row indices");
+    if (!knn_ids || !knn_sq || !core_sq || !labels || !mst_src || !mst_dst || !mst_wsq)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "null buffer");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    FitWorkspace *f = ctx->fit;
+    ForestBuffers &b = f->forest;
+    int rc = forest_reserve(ctx, b, n, d);
+    if (rc) return rc;
+    const int k = (int)((int64_t)min_samples < n - 1 ? min_samples : n - 1);
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(b.status, 0, sizeof(DevStatus), s));
+    if ((rc = forest_core(ctx, knn_sq, n, k, min_samples, core_sq, s))) return rc;
+    if ((rc = forest_seed(ctx, b, core_sq, knn_ids, knn_sq, n, k, labels, mst_src, mst_dst,
+                          mst_wsq, s)))
+        return rc;
+    DevStatus *hs = f->host_status;
+    if ((rc = read_status(ctx, b.status, hs, s))) return rc;
+    if (hs->err_kind) return status_error(ctx, hs->err_kind);
+    if (n_edges) *n_edges = (int64_t)hs->edges;
+    if (components) *components = (int64_t)hs->components;
+    return CUSCAN_OK;
+}
+
+int cuscan_shard_round_keys(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                            const int32_t *labels, int64_t n, int32_t d, int64_t row_begin,
+                            int64_t row_end, uint64_t *row_keys, void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n <= 0 || d <= 0 || row_begin < 0 || row_end > n || row_begin > row_end || !row_keys)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "row range [%lld, %lld) outside the %lld rows",
+                    (long long)row_begin, (long long)row_end, (long long)n);
+    if (n > INT32_MAX - 1) return fail(ctx, CUSCAN_OVERFLOW, "row indices");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    FitWorkspace *f = ctx->fit;
+    int rc = ensure(ctx, f->op_tiles_lo, sizeof(int32_t) * (ceil_div(n, 32) + 1), "tiles");
+    if (!rc) rc = ensure(ctx, f->op_tiles_hi, sizeof(int32_t) * (ceil_div(n, 32) + 1), "tiles");
+    if (rc) return rc;
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(row_keys);
+    if ((rc = launch_fill_u64(ctx, keys, n, ~0ull, s))) return rc;
+    if (row_end == row_begin) return CUSCAN_OK;
+    return launch_candidates_fp32(ctx, data, core_sq, labels, nullptr, n, d, keys,
+                                  as<int32_t>(f->op_tiles_lo), as<int32_t>(f->op_tiles_hi), s,
+                                  nullptr, row_end - row_begin, row_begin);
+}
+
+int cuscan_shard_round_merge(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                             int32_t *labels, int64_t n, int32_t d, const uint64_t *row_keys,
+                             uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                             int64_t *n_edges, int64_t *components, double *mst_weight,
+                             void *stream) {
+    if (!ctx) return CUSCAN_INVALID_INPUT;
+    clear_error(ctx);
+    if (n < 2 || d <= 0 || !row_keys) return fail(ctx, CUSCAN_INVALID_INPUT, "bad round input");
+    CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    FitWorkspace *f = ctx->fit;
+    ForestBuffers &b = f->forest;
+    if (!b.status) return fail(ctx, CUSCAN_INVALID_INPUT, "no shard seed on this context");
+    DevStatus *hs = f->host_status;
+    int rc = read_status(ctx, b.status, hs, s);
+    if (rc) return rc;
+    const int64_t before = (int64_t)hs->components;
+    if (before > 1) {
+        if ((rc = forest_sort_by_component(ctx, b, data, core_sq, labels, n, d, s))) return rc;
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(b.row_keys.ptr, row_keys, sizeof(uint64_t) * n,
+                                         cudaMemcpyDeviceToDevice, s));
+        if ((rc = forest_round(ctx, b, n, before, labels, mst_src, mst_dst, mst_wsq, s, 0)))
+            return rc;
+        if ((rc = read_status(ctx, b.status, hs, s))) return rc;
+        if (hs->err_kind) return status_error(ctx, hs->err_kind);
+    }
+    if (hs->components == 1 && mst_weight) {
+        if ((rc = forest_mst_weight(ctx, b, mst_wsq, (int64_t)hs->edges, s))) return rc;
+        CUSCAN_CUDA(ctx, cudaMemcpyAsync(&hs->mst_weight, &b.status->mst_weight, sizeof(double),
+                                         cudaMemcpyDeviceToHost, s));
+        CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+        *mst_weight = hs->mst_weight;
+    }
+    if (n_edges) *n_edges = (int64_t)hs->edges;
+    if (components) *components = (int64_t)hs->components;
+    return CUSCAN_OK;
+}
+
 int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
-                                      int32_t operands, float *tile_out, float *scale_out,
-                                      void *stream) {
+                                      int32_t operands, float *tile_out, float *rows_out,
+                                      float *scale_out, void *stream) {
     if (!ctx) return CUSCAN_INVALID_INPUT;
     clear_error(ctx);
     if (n < 256 || d <= 0 || !data || !tile_out)
         return fail(ctx, CUSCAN_INVALID_INPUT, "debug tile needs n >= 256 rows");
-    if (operands < 0 || operands > 1)
+    if (operands < 0 || operands > 2)
         return fail(ctx, CUSCAN_INVALID_INPUT, "unknown operand format");
     CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = pick_stream(ctx, stream);
     int rc = forest_reserve(ctx, ctx->fit->forest, n, d);
     if (rc) return rc;
-    return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, operands, tile_out, scale_out, s);
+    return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, operands, tile_out, rows_out,
+                             scale_out, s);
 }
 
 int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
                              float *tile_out, void *stream) {
-    return cuscan_debug_screen_tile_operands(ctx, data, n, d, 0, tile_out, nullptr, stream);
+    return cuscan_debug_screen_tile_operands(ctx, data, n, d, 0, tile_out, nullptr, nullptr,
+                                             stream);
 }
 
 }  // extern "C"

@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
     const float *__restrict__ data, const float *__restrict__ core,
     const int32_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n, int d,
     const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t ref_chunk,
-    unsigned long long *__restrict__ row_keys, const int32_t *__restrict__ qmap, int64_t nq) {
+    unsigned long long *__restrict__ row_keys, const int32_t *__restrict__ qmap, int64_t nq,
+    int64_t qoff) {
     extern __shared__ __align__(16) float smem[];
     float *qs = smem;                       // [d][QB]
     float *tiles = smem + (size_t)d * QB;   // 2 x [d][RTP]
@@ -91,9 +92,9 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
     int64_t r_end = r_begin + ref_chunk;
     if (r_end > n) r_end = n;
 
-    // query rows are positions qmap[qi] (or qi) of the same arrays
+    // query rows are positions qmap[qi] (or qoff + qi) of the same arrays
     const bool q_valid = qi < nq;
-    const int64_t qpos = q_valid ? (qmap ? (int64_t)qmap[qi] : qi) : 0;
+    const int64_t qpos = q_valid ? (qmap ? (int64_t)qmap[qi] : qoff + qi) : 0;
     const int32_t my_label = q_valid ? labels[qpos] : -1;
     const float my_core = q_valid ? core[qpos] : 0.0f;
     if (tid == 0) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
         int q = e / d;
         int f = e - q * d;
         int64_t row = q0 + q;
-        int64_t src = row < nq ? (qmap ? (int64_t)qmap[row] : row) : 0;
+        int64_t src = row < nq ? (qmap ? (int64_t)qmap[row] : qoff + row) : 0;
         qs[f * QB + q] = row < nq ? data[src * (int64_t)d + f] : 0.0f;
     }
     __syncthreads();
@@ -317,8 +318,8 @@ int launch_tile_ranges(cuscan_ctx *ctx, const int32_t *labels, int64_t n, int32_
 int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core_sq,
                            const int32_t *labels, const int32_t *ids, int64_t n, int d,
                            unsigned long long *row_keys, int32_t *tile_lo, int32_t *tile_hi,
-                           cudaStream_t s, const int32_t *qmap, int64_t nq) {
-    if (!qmap) nq = n;
+                           cudaStream_t s, const int32_t *qmap, int64_t nq, int64_t qoff) {
+    if (!qmap && qoff == 0 && nq == 0) nq = n;
     if (nq == 0) return CUSCAN_OK;
     int rc = launch_tile_ranges(ctx, labels, n, tile_lo, tile_hi, s);
     if (rc) return rc;
@@ -340,7 +341,7 @@ int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core
     if (int rc = allow_dynamic_smem(ctx, candidates_fp32_kernel, smem)) return rc;
     dim3 grid((unsigned)qblocks, (unsigned)splits);
     CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d,
-                  tile_lo, tile_hi, chunk, row_keys, qmap, nq);
+                  tile_lo, tile_hi, chunk, row_keys, qmap, nq, qoff);
     CUSCAN_LAUNCH(ctx, "candidates_fp32_kernel");
     return CUSCAN_OK;
 }

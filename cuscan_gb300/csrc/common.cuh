@@ -188,11 +188,13 @@ size_t exact_knn_scratch_elems(const cuscan_ctx *ctx, int64_t nq, int64_t nr, in
 // minimised atomically into row_keys[] (which the caller fills with ~0 first). Rows are
 // positions in `data`; ids maps a position to the original id used for tie-breaking and
 // output (NULL = identity). tile_lo/tile_hi are scratch of ceil(n/32) ints each.
-// With qmap, only the nq query positions qmap[0..nq) are scanned (against all n positions).
+// With qmap, only the nq query positions qmap[0..nq) are scanned (against all n positions);
+// without it, the positions [qoff, qoff + nq) (all n positions when nq and qoff are 0).
 int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core_sq,
                            const int32_t *labels, const int32_t *ids, int64_t n, int d,
                            unsigned long long *row_keys, int32_t *tile_lo, int32_t *tile_hi,
-                           cudaStream_t s, const int32_t *qmap = nullptr, int64_t nq = 0);
+                           cudaStream_t s, const int32_t *qmap = nullptr, int64_t nq = 0,
+                           int64_t qoff = 0);
 // Label range (min, max) of every 32-row tile of `labels`.
 int launch_tile_ranges(cuscan_ctx *ctx, const int32_t *labels, int64_t n, int32_t *tile_lo,
                        int32_t *tile_hi, cudaStream_t s);

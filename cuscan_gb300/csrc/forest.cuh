@@ -29,11 +29,14 @@ struct RefinedBuffers {
     Buffer urow, colcnt, colbuf;  // symmetric Borůvka: row bounds, column-side buffers
     Buffer act_flag, act_idx, act_pos;  // Borůvka rows that can hold their component's edge
     Buffer rowlb, lbtmp;  // lower bounds of each row's cheapest cross edge (original order)
+    Buffer cursor;        // tiles issued by the CTAs of the running screen (shared tile order)
     // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
     bool want_fp16 = false;  // requested by the caller's precision
     bool fp16 = false;       // in use (the data's range allows a scale)
+    bool split = false;      // split-bf16 operands (hi + lo) in use for the current fit
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;
+    float amax_value = 0.0f; // largest |x| of the current fit
     bool range_ok = true;    // the current fit's values keep every screen quantity finite
     int64_t tile_pairs = 0;  // (query block, tile) pairs the screens of the current fit ran
     int64_t screened_rows = 0;  // query rows of the current fit's Borůvka screens
@@ -62,7 +65,7 @@ struct ForestBuffers {
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
 void forest_release(ForestBuffers &b);
 // Every device buffer of the forest and of the bf16 screen (out may be null); returns the count.
-constexpr int kForestBufferCount = 60;
+constexpr int kForestBufferCount = 61;
 int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);

@@ -468,6 +468,7 @@ extern "C" int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, i
         S.components_after_seed = (int64_t)hs.components_after_seed;
         S.cross_pairs = hs.cross_pairs;
         S.mst_weight = hs.mst_weight;
+        S.operand_format = -1;  // packed fits run the exact kernels
     }
     clear_error(ctx);
     if (first) {

@@ -17,6 +17,14 @@
 // when it is larger than the selected exact value no outside pair can change the result. Rows
 // that fail the check are re-run by the exact f32 kernels. The outputs are therefore bit
 // identical to the plain path.
+//
+// Operand formats: bf16 of x; fp16 of x * 2^k (a power-of-two scale that brings the largest
+// |x| into [2^14, 2^15)); and split bf16, x = hi + lo with hi = bf16(x) and lo = bf16(x - hi),
+// whose dot product hi.hi' + hi.lo' + lo.hi' (three K blocks per 64 features) misses x.y by
+// about 3 * 2^-16 |x||y| instead of 2^-7. A bf16-refined fit whose plain bf16 screen leaves too
+// many kNN rows inconclusive screens again with split bf16 (d <= 64, where a tile of hi and lo
+// blocks fits two pipeline stages) or with scaled fp16 operands (wider rows), and keeps that
+// format for its Borůvka rounds.
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -45,6 +53,11 @@ constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row ha
 
 struct Params {
     const uint8_t *xt;        // 16-bit tiles, pre-swizzled (see tile_16bit_kernel)
+    int nbk;                  // K blocks per tile row of the copy: kblocks, or 2 kblocks (split)
+    int split;                // split bf16: blocks [0, kblocks) hold hi, [kblocks, 2 kblocks) lo
+    // tiles issued by all CTAs so far: a query block starts its sweep of the shared tile order
+    // where the other CTAs are, so that the tiles they stream stay in L2
+    unsigned long long *cursor;
     const float *pnorm;       // [n_pad] f32 squared norms (+inf on padding rows)
     const float *mnorm;       // [n_pad] norms rounded up (0 on padding rows)
     const float *core;        // [n] core distances (Borůvka)
@@ -101,6 +114,13 @@ constexpr double SYM_ACTIVE_MIN = 0.9;  // smallest share of screened rows for t
 constexpr int KNN_CAP = 512;  // threshold-mode candidate slots per row half
 constexpr int KNN_LIST = 22;  // kNN list entries per row half
 constexpr int RESCREEN_MIN_ROWS = 256;  // fewer inconclusive kNN rows go straight to exact f32
+// A bf16-refined fit whose first kNN screen leaves more than this share of rows inconclusive
+// screens again with tighter operands (split bf16, or scaled fp16 for rows too wide to split).
+constexpr double TIGHTEN_TRIGGER = 0.15;
+// Operand formats of the 16-bit copy.
+constexpr int FMT_BF16 = 0;
+constexpr int FMT_FP16 = 1;
+constexpr int FMT_SPLIT = 2;
 
 // ---- PTX wrappers ----
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -216,44 +236,55 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
                    "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
 }
 
-// Byte offset of element (row r, feature f) in the tiled bf16 copy: 256-row tiles, each split
-// into 64-feature K blocks of 256 rows x 128 bytes whose 16-byte chunks are XOR-swizzled by the
-// row (the SWIZZLE_128B K-major layout), so one bulk copy lands a block ready for the MMA.
-__host__ __device__ __forceinline__ uint64_t tiled_offset(int64_t r, int f, int d_pad) {
+// Byte offset of element (row r, column f < d_eff) in the tiled 16-bit copy: 256-row tiles, each
+// split into 64-column K blocks of 256 rows x 128 bytes whose 16-byte chunks are XOR-swizzled
+// by the row (the SWIZZLE_128B K-major layout), so one bulk copy lands a block ready for the
+// MMA. d_eff is d_pad, or 2 d_pad for split copies (the lo parts in columns d_pad + f).
+__host__ __device__ __forceinline__ uint64_t tiled_offset(int64_t r, int f, int d_eff) {
     const int64_t t = r >> 8;
     const int rr = (int)(r & 255);
     const int kb = f >> 6, c = f & 63;
     const int chunk = (c >> 3) ^ (rr & 7);
-    return (uint64_t)t * (uint64_t)(BN * d_pad * 2) + (uint64_t)kb * KBLOCK_B +
+    return (uint64_t)t * (uint64_t)(BN * d_eff * 2) + (uint64_t)kb * KBLOCK_B +
            (uint64_t)rr * 128 + (uint64_t)chunk * 16 + (uint64_t)(c & 7) * 2;
 }
 
-// 16-bit tiled copy of the (scaled) rows: bf16, or fp16 of x * scale (scale a power of two).
+// 16-bit tiled copy of the (scaled) rows: bf16, fp16 of x * scale (scale a power of two), or
+// split bf16 (hi in columns [0, d_pad), lo = bf16(x - hi) in [d_pad, 2 d_pad)).
 // Row r of the copy is row rowmap[r] of x (r itself when rowmap is null); rows >= n are zero.
-template <bool FP16>
+template <int FMT>
 __global__ void tile_16bit_kernel(const float *__restrict__ x, int64_t n, int d, int d_pad,
                                   int64_t n_pad, float scale, const int32_t *__restrict__ rowmap,
                                   uint8_t *__restrict__ xt) {
-    // one thread per (row, group of 8 features): 16 bytes out
+    // one thread per (row, group of 8 features): 16 bytes out (32 for split)
     const int groups = d_pad >> 3;
+    const int d_eff = FMT == FMT_SPLIT ? 2 * d_pad : d_pad;
     int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_pad * groups) return;
     int64_t r = e / groups;
     int g = (int)(e - r * groups);
     const int64_t src = r < n ? (rowmap ? (int64_t)rowmap[r] : r) : 0;
     __align__(16) uint16_t h[8];
+    __align__(16) uint16_t l[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         int f = g * 8 + q;
         float v = (r < n && f < d) ? x[src * d + f] : 0.0f;
-        if constexpr (FP16) {
+        if constexpr (FMT == FMT_FP16) {
             h[q] = __half_as_ushort(__float2half_rn(v * scale));
         } else {
-            h[q] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+            const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+            h[q] = __bfloat16_as_ushort(hi);
+            // v - hi is exact in f32 (hi is within a factor of two of v)
+            if constexpr (FMT == FMT_SPLIT)
+                l[q] = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(hi)));
         }
     }
-    *reinterpret_cast<uint4 *>(xt + tiled_offset(r, g * 8, d_pad)) =
+    *reinterpret_cast<uint4 *>(xt + tiled_offset(r, g * 8, d_eff)) =
         *reinterpret_cast<const uint4 *>(h);
+    if constexpr (FMT == FMT_SPLIT)
+        *reinterpret_cast<uint4 *>(xt + tiled_offset(r, d_pad + g * 8, d_eff)) =
+            *reinterpret_cast<const uint4 *>(l);
 }
 
 // Squared norms and rounded-up norms of the scaled rows (x * scale, exact for a power of two);
@@ -313,8 +344,10 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
 
 // Order in which query block qb visits the reference tiles: first a window of WARM tiles around
 // the block's own tile (in cell-sorted data these hold the block's nearest neighbours, so the
-// per-row thresholds tighten at once), then every other tile in one global order shared by all
-// CTAs, so that the blocks running at the same time stream the same tiles and share them in L2.
+// per-row thresholds tighten at once), then every other tile in one cyclic order shared by all
+// CTAs, entered at the rotation `rot` the producer chose when the block started: where the
+// CTAs are on average, so that blocks that start at different times still stream the same
+// tiles and share them in L2.
 constexpr int64_t WARM = 4;
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float r;
@@ -357,10 +390,12 @@ __device__ __forceinline__ int64_t window_start(const Params &P, int64_t qb) {
     if (a > P.n_tiles - w) a = P.n_tiles - w;
     return a;
 }
-__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_t i) {
+__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_t rot, int64_t i) {
     const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
     if (i < w) return a + i;
-    const int64_t j = i - w;
+    const int64_t rest = P.n_tiles - w;  // > 0 here; rot < rest
+    int64_t j = i - w + rot;
+    if (j >= rest) j -= rest;
     return j < a ? j : j + w;
 }
 
@@ -372,8 +407,9 @@ __device__ __forceinline__ int64_t vis_count(const Params &P, int64_t qb) {
     return SYM ? P.n_tiles - (qb >> 1) : P.n_tiles;
 }
 template <bool SYM>
-__device__ __forceinline__ int64_t vis_tile(const Params &P, int64_t qb, int64_t wa, int64_t i) {
-    return SYM ? (qb >> 1) + i : tile_order(P, wa, i);
+__device__ __forceinline__ int64_t vis_tile(const Params &P, int64_t qb, int64_t wa,
+                                            int64_t rot, int64_t i) {
+    return SYM ? (qb >> 1) + i : tile_order(P, wa, rot, i);
 }
 
 // The query block a CTA takes at its qi-th step (blocks in order, strided over the CTAs).
@@ -430,8 +466,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     constexpr bool APPEND = BORUVKA || THRESH;  // threshold modes append to per-row buffers
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const uint32_t a_bytes = (uint32_t)P.kblocks * KBLOCK_A;
-    const uint32_t b_bytes = (uint32_t)P.kblocks * KBLOCK_B;
+    const uint32_t a_bytes = (uint32_t)P.nbk * KBLOCK_A;
+    const uint32_t b_bytes = (uint32_t)P.nbk * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
     float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][PB_STRIDE]
@@ -444,8 +480,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     uint64_t *t_full = a_full + 2;   // [2]
     uint64_t *t_empty = a_full + 4;  // [2]
     uint64_t *done = a_full + 6;     // MMA drain on the abort path
-    uint32_t *tmem_slot = (uint32_t *)(a_full + 7);
+    uint64_t *rot_full = a_full + 7;    // [4]: the producer published a block's rotation
+    uint64_t *rot_empty = a_full + 11;  // [4]: every epilogue warp has read it
+    uint32_t *tmem_slot = (uint32_t *)(a_full + 15);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
+    int64_t *rot_val = (int64_t *)(tmem_slot + 2);  // [4]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -459,6 +498,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         for (int b = 0; b < 2; ++b) {
             mbar_init(&t_full[b], 1);
             mbar_init(&t_empty[b], EPI_WARPS);
+        }
+        for (int r = 0; r < 4; ++r) {
+            mbar_init(&rot_full[r], 1);
+            mbar_init(&rot_empty[r], EPI_WARPS);
         }
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -483,7 +526,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             // parity of the last fill of each stage (bit 1 set = a fill was issued)
             uint32_t issued[4] = {0, 0, 0, 0};
             uint32_t a_issued = 0;
-            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
+            uint32_t li = 0;  // this CTA's query step
+            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x, ++li) {
                 const int64_t qb = block_at<SYM>(P, qi);
                 if (!mbar_wait(a_empty, a_phase ^ 1, abort, P.error)) break;
                 a_issued = 2u | a_phase;
@@ -491,27 +535,39 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 mbar_expect_tx(a_full, a_bytes);
                 const uint8_t *asrc = P.xq + (uint64_t)(qb >> 1) * (uint64_t)b_bytes +
                                       (uint64_t)(qb & 1) * KBLOCK_A;
-                for (int kb = 0; kb < P.kblocks; ++kb)
+                for (int kb = 0; kb < P.nbk; ++kb)
                     bulk_g2s(sA + kb * KBLOCK_A, asrc + (uint64_t)kb * KBLOCK_B, KBLOCK_A, a_full);
+                // this block's rotation of the shared tile order: the average position of the
+                // CTAs (tiles issued so far over the grid), published to the epilogue warps
+                int64_t rot = 0;
+                if (!SYM && P.n_tiles > WARM) {
+                    const unsigned long long all = *(volatile unsigned long long *)P.cursor;
+                    rot = (int64_t)((all / gridDim.x) % (unsigned long long)(P.n_tiles - WARM));
+                }
+                const uint32_t rs = li & 3;
+                if (!mbar_wait(&rot_empty[rs], ((li >> 2) & 1) ^ 1, abort, P.error)) break;
+                rot_val[rs] = rot;
+                mbar_arrive(&rot_full[rs]);
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
                 for (int64_t i = 0; i < nvis; ++i) {
-                    const int64_t t = vis_tile<SYM>(P, qb, wa, i);
+                    const int64_t t = vis_tile<SYM>(P, qb, wa, rot, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
                     issued[stage] = 2u | phase;
                     mbar_expect_tx(&full[stage], b_bytes);
                     const uint8_t *bsrc = P.xt + (uint64_t)t * (uint64_t)b_bytes;
                     uint8_t *bdst = sB + (size_t)stage * b_bytes;
-                    for (int kb = 0; kb < P.kblocks; ++kb)
+                    for (int kb = 0; kb < P.nbk; ++kb)
                         bulk_g2s(bdst + kb * KBLOCK_B, bsrc + (uint64_t)kb * KBLOCK_B, KBLOCK_B,
                                  &full[stage]);
                     if (++stage == P.stages) {
                         stage = 0;
                         phase ^= 1;
                     }
+                    atomicAdd(P.cursor, 1ull);
                 }
             }
             if (*abort) {
@@ -540,11 +596,13 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
+                // the set of tiles the block runs does not depend on their order: visit them in
+                // the unrotated order to count the skipped ones
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
                 bool ok = true;
                 for (int64_t i = 0; i < nvis; ++i) {
-                    const int64_t t = vis_tile<SYM>(P, qb, wa, i);
+                    const int64_t t = vis_tile<SYM>(P, qb, wa, 0, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                     if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
@@ -559,6 +617,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                             const uint64_t ad = desc_sw128(a_base + kb * KBLOCK_A + ks * 32);
                             const uint64_t bd = desc_sw128(bstage + kb * KBLOCK_B + ks * 32);
                             mma_16bit(d_tmem, ad, bd, P.idesc, (kb | ks) != 0);
+                        }
+                        if (P.split) {
+                            // lo x hi and hi x lo (blocks kblocks + kb hold the lo parts)
+                            const uint32_t lo = (uint32_t)(P.kblocks + kb);
+#pragma unroll
+                            for (int ks = 0; ks < 4; ++ks) {
+                                mma_16bit(d_tmem, desc_sw128(a_base + lo * KBLOCK_A + ks * 32),
+                                          desc_sw128(bstage + kb * KBLOCK_B + ks * 32), P.idesc, 1u);
+                                mma_16bit(d_tmem, desc_sw128(a_base + kb * KBLOCK_A + ks * 32),
+                                          desc_sw128(bstage + lo * KBLOCK_B + ks * 32), P.idesc, 1u);
+                            }
                         }
                     }
                     mma_commit(&empty[stage]);
@@ -597,6 +666,14 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         uint32_t tcount = 0;
         for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
             const int64_t qb = block_at<SYM>(P, qi);
+            // the block's rotation of the tile order, published by the producer (li: this
+            // CTA's query step)
+            const uint32_t li = (uint32_t)((qi - blockIdx.x) / gridDim.x);
+            const uint32_t rs = li & 3;
+            if (!mbar_wait(&rot_full[rs], (li >> 2) & 1, abort, P.error)) break;
+            const int32_t rot = (int32_t)*(volatile int64_t *)&rot_val[rs];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&rot_empty[rs]);
             const int64_t row = qb * BM + row_local;  // query row
             const bool valid = row < P.nq;
             const int64_t self = valid && P.qpos ? (int64_t)P.qpos[row] : row;
@@ -642,7 +719,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             }
             // next visited position i (>= i0) in this block's tile order
             auto next_index = [&](int64_t i) -> int64_t {
-                while (i < nvis && tile_skipped<BORUVKA>(P, vis_tile<SYM>(P, qb, wa, i), qlo, qhi)) ++i;
+                while (i < nvis && tile_skipped<BORUVKA>(P, vis_tile<SYM>(P, qb, wa, rot, i), qlo, qhi)) ++i;
                 return i;
             };
             // per-tile column data, fetched one tile ahead
@@ -681,10 +758,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
             };
             int64_t ti = next_index(0);
-            if (ti < nvis) prefetch(vis_tile<SYM>(P, qb, wa, ti));
+            if (ti < nvis) prefetch(vis_tile<SYM>(P, qb, wa, rot, ti));
             bool ok = true;
             while (ti < nvis) {
-                const int64_t t = vis_tile<SYM>(P, qb, wa, ti);
+                const int64_t t = vis_tile<SYM>(P, qb, wa, rot, ti);
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
@@ -732,7 +809,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
-                if (ti_next < nvis) prefetch(vis_tile<SYM>(P, qb, wa, ti_next));
+                if (ti_next < nvis) prefetch(vis_tile<SYM>(P, qb, wa, rot, ti_next));
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -1389,29 +1466,47 @@ __global__ void fill_u32_kernel(uint32_t *p, int64_t n, uint32_t v) {
     if (i < n) p[i] = v;
 }
 
-// Error bound coefficients for d features (K = padded depth of the 16-bit dot product).
-// bf16: unit roundoff 2^-8 over the whole f32 range. fp16: unit roundoff 2^-11 for the scaled
-// values (|x * scale| <= 2^15, so nothing overflows); scaled values below 2^-14 round in the
-// subnormal range with an absolute error of at most 2^-25, which adds at most
-// 2 * [2^-25 (1 + u) sqrt(d) (m_i + m_j) + d 2^-50] to the distance; with every scaled norm at
-// most sqrt(d) 2^15 this is bounded by the constant abs_c.
-void error_coefficients(int d, int d_pad, bool fp16, float &c_a, float &c_b, float &abs_c) {
+// Error bound coefficients of one operand format (fmt) at d features, K blocks of 64 (d_pad).
+//  * Operands: unit roundoff u = 2^-8 (bf16) or 2^-11 (fp16 of the scaled values; |x * scale|
+//    <= 2^15, so nothing overflows). Split bf16 represents x = hi + lo + e with |e| <= u^2 |x|,
+//    so hi.hi' + hi.lo' + lo.hi' misses x.y by at most u^2 (3 + 4u) |x||y| per feature instead
+//    of (2u + u^2) |x||y|.
+//  * Accumulation: the K products of an entry (d_pad, or 3 d_pad for split operands) are
+//    assumed to come out of the tensor core's f32 accumulation within K 2^-23 of the sum of
+//    their magnitudes, two f32 units in the last place per product where f32 sequential
+//    summation needs one. tests/test_gpu_accumulation.py drives the accumulator with
+//    adversarial operands and requires the observed worst case to stay within a quarter of it.
+//  * C_B: norms and the reference sum each carry at most (d + 2) f32 roundings; the epilogue
+//    adds a few more; everything is taken three times over.
+//  * abs_c: scaled fp16 values below 2^-14 round in the subnormal range with an absolute error
+//    of at most 2^-25, which adds at most 2 [2^-25 (1 + u) sqrt(d) (m_i + m_j) + d 2^-50] to the
+//    distance; with every scaled norm at most sqrt(d) 2^15 this is a constant. bf16 values (hi,
+//    lo) in the subnormal range, or flushed to zero, err by at most 2^-126 each.
+void error_coefficients(int d, int d_pad, int fmt, float absmax, float &c_a, float &c_b,
+                        float &abs_c) {
+    const bool fp16 = fmt == FMT_FP16;
     const double u = std::ldexp(1.0, fp16 ? -11 : -8);  // unit roundoff (round to nearest)
     const double u32 = std::ldexp(1.0, -24);            // f32 unit roundoff
-    // rounding of both factors, plus a generous bound on the tensor-core f32 accumulation
-    // (each of K partial sums off by at most 2^-21 of the running magnitude)
-    const double a1 = (2.0 * u + u * u) + (double)d_pad * std::ldexp(1.0, -21) * (1 + u) * (1 + u);
-    // norms and the reference sum each carry at most (d + 2) f32 roundings; the epilogue adds a
-    // few more; everything is taken three times over
+    const double K = fmt == FMT_SPLIT ? 3.0 * d_pad : (double)d_pad;
+    double rnd, mag;
+    if (fmt == FMT_SPLIT) {
+        rnd = u * u * (3.0 + 4.0 * u);
+        mag = (1 + u) * (1 + u) * (1 + 2 * u * (1 + u));
+    } else {
+        rnd = 2.0 * u + u * u;
+        mag = (1 + u) * (1 + u);
+    }
+    const double a1 = rnd + K * std::ldexp(1.0, -23) * mag;
     const double b = 3.5 * (double)(d + 4) * u32 + 1e-7;
     c_a = (float)(2.0 * a1 * (1.0 + 1e-4));
     c_b = (float)b;
-    abs_c = 0.0f;
+    const double dd = (double)d;
     if (fp16) {
         const double eta = std::ldexp(1.0, -25);
-        const double m_max = std::sqrt((double)d) * std::ldexp(1.0, 15);
-        abs_c = (float)(2.0 * (eta * (1 + u) * std::sqrt((double)d) * 2.0 * m_max +
-                               (double)d * eta * eta) * 1.01);
+        const double m_max = std::sqrt(dd) * std::ldexp(1.0, 15);
+        abs_c = (float)(2.0 * (eta * (1 + u) * std::sqrt(dd) * 2.0 * m_max + dd * eta * eta) * 1.01);
+    } else {
+        abs_c = (float)(std::ldexp(1.0, -126) * (8.0 * dd * (double)absmax * 1.01 + 2.0 * K));
     }
 }
 
@@ -1433,18 +1528,23 @@ int refined_available() { return 1; }
 
 struct Layout {
     int d_pad, kblocks, stages;
+    int nbk, split;  // K blocks per tile row of the copy; split bf16 copy
     int64_t n_pad, n_tiles, n_qblocks;
     size_t smem;
 };
 
-static bool refined_layout(int64_t n, int d, Layout &L) {
+// Tiling of n rows of d features; split copies hold hi and lo blocks, so a tile (the unit of a
+// pipeline stage) is twice as large and fits two stages only for d <= 64.
+static bool refined_layout(int64_t n, int d, Layout &L, bool split = false) {
     L.d_pad = (int)ceil_div(d, 64) * 64;
     if (L.d_pad > 128) return false;
     L.kblocks = L.d_pad / 64;
+    L.split = split ? 1 : 0;
+    L.nbk = split ? 2 * L.kblocks : L.kblocks;
     L.n_tiles = ceil_div(n, BN);
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
-    const size_t a = (size_t)L.kblocks * KBLOCK_A, b = (size_t)L.kblocks * KBLOCK_B;
+    const size_t a = (size_t)L.nbk * KBLOCK_A, b = (size_t)L.nbk * KBLOCK_B;
     const size_t fixed = a + (size_t)EPI_WARPS * PB_STRIDE * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
                          256 + 1024;
     int st = (int)((227 * 1024 - fixed) / b);
@@ -1464,15 +1564,17 @@ size_t refined_workspace_bytes(int64_t n, int d, int k) {
     Layout L;
     if (!refined_shape_ok(n, d, k) || !refined_layout(n, d, L)) return 0;
     constexpr size_t M = 32;
-    size_t b = (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;  // xt, norms
-    b += 3 * sizeof(float) * (size_t)L.n_tiles + 48;          // tile stats, flags, range
+    // a bf16-refined fit may switch to split copies (twice the columns) when d <= 64
+    const size_t copy_cols = (size_t)L.d_pad * (L.d_pad <= 64 ? 2 : 1);
+    size_t b = (size_t)L.n_pad * copy_cols * 2 + 2 * sizeof(float) * (size_t)L.n_pad;  // xt, norms
+    b += 3 * sizeof(float) * (size_t)L.n_tiles + 64;          // tile stats, flags, cursor
     b += sizeof(int32_t) * (size_t)n;                                                 // fallback
     b += 2 * 4 * (size_t)n * 2 * M;                  // candidate ids and bounds (two lists of M)
     b += sizeof(uint32_t) * (size_t)n + 2 * sizeof(int32_t) * (size_t)n;  // cbound, rowcnt
     b += 256 * sizeof(float) * (size_t)d + 8 * (size_t)n;                 // pivots, cells
     // threshold re-screen of inconclusive kNN rows (at most all n): thresholds, tiles, norms,
     // candidates, counts, fallback list
-    b += 4 * (size_t)n + (size_t)L.n_pad * L.d_pad * 2 + 2 * sizeof(float) * (size_t)L.n_pad;
+    b += 4 * (size_t)n + (size_t)L.n_pad * copy_cols * 2 + 2 * sizeof(float) * (size_t)L.n_pad;
     b += 4 * (size_t)n * 2 * KNN_CAP + 8 * (size_t)n + 4 * (size_t)n;
     // symmetric Borůvka: row bounds, column-side counts and candidates; subset rounds: flags,
     // their scan and the gathered positions
@@ -1486,12 +1588,16 @@ static int tile_rows(cuscan_ctx *ctx, const RefinedBuffers &R, const float *x, i
                      int d_pad, int64_t n_pad, const int32_t *rowmap, uint8_t *xt, float *pnorm,
                      float *mnorm, cudaStream_t s) {
     const int64_t groups = n_pad * (d_pad / 8);
+    const unsigned gb = (unsigned)ceil_div(groups, 256);
     if (R.fp16)
-        CUSCAN_KERNEL(tile_16bit_kernel<true>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n, d,
-                      d_pad, n_pad, R.scale, rowmap, xt);
+        CUSCAN_KERNEL(tile_16bit_kernel<FMT_FP16>, gb, 256, 0, s, x, n, d, d_pad, n_pad, R.scale,
+                      rowmap, xt);
+    else if (R.split)
+        CUSCAN_KERNEL(tile_16bit_kernel<FMT_SPLIT>, gb, 256, 0, s, x, n, d, d_pad, n_pad, 1.0f,
+                      rowmap, xt);
     else
-        CUSCAN_KERNEL(tile_16bit_kernel<false>, (unsigned)ceil_div(groups, 256), 256, 0, s, x, n,
-                      d, d_pad, n_pad, 1.0f, rowmap, xt);
+        CUSCAN_KERNEL(tile_16bit_kernel<FMT_BF16>, gb, 256, 0, s, x, n, d, d_pad, n_pad, 1.0f,
+                      rowmap, xt);
     CUSCAN_KERNEL(norms_kernel, (unsigned)ceil_div(n_pad, 256), 256, 0, s, x, n, d, n_pad,
                   R.fp16 ? R.scale : 1.0f, rowmap, pnorm, mnorm);
     CUSCAN_LAUNCH(ctx, "16-bit tiles");
@@ -1500,7 +1606,7 @@ static int tile_rows(cuscan_ctx *ctx, const RefinedBuffers &R, const float *x, i
 
 static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float *x, int64_t n,
                 int d, const int32_t *chunk_lo, const int32_t *chunk_hi, cudaStream_t s) {
-    int rc = ensure(ctx, R.xt, (size_t)L.n_pad * L.d_pad * 2, "bf16 tiles");
+    int rc = ensure(ctx, R.xt, (size_t)L.n_tiles * L.nbk * KBLOCK_B, "16-bit tiles");
     if (!rc) rc = ensure(ctx, R.pnorm, sizeof(float) * L.n_pad, "norms");
     if (!rc) rc = ensure(ctx, R.mnorm, sizeof(float) * L.n_pad, "norms");
     if (!rc) rc = ensure(ctx, R.tile_mmax, sizeof(float) * L.n_tiles, "tile norms");
@@ -1508,6 +1614,7 @@ static int prep(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float
     if (!rc) rc = ensure(ctx, R.tile_hi, sizeof(int32_t) * L.n_tiles, "tile labels");
     if (!rc) rc = ensure(ctx, R.error, 16, "error flag");
     if (!rc) rc = ensure(ctx, R.count, 16, "fallback count");
+    if (!rc) rc = ensure(ctx, R.cursor, 16, "tile cursor");
     if (!rc) rc = ensure(ctx, R.fallback, sizeof(int32_t) * n, "fallback rows");
     if (!rc) rc = ensure(ctx, R.qthr, sizeof(float) * n, "fallback thresholds");
     if (rc) return rc;
@@ -1535,6 +1642,7 @@ static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, i
                            cudaStream_t s) {
     if (R.have_scale) return CUSCAN_OK;
     R.fp16 = false;
+    R.split = false;
     R.scale = 1.0f;
     R.range_ok = true;
     int rc = ensure(ctx, R.absmax, 16, "range reduction");
@@ -1552,6 +1660,7 @@ static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, i
     float amax;
     memcpy(&amax, &bits, sizeof(amax));
     R.range_ok = std::isfinite(amax) && (double)d * (double)amax * (double)amax <= kScreenRangeMax;
+    R.amax_value = std::isfinite(amax) ? amax : 0.0f;
     if (R.want_fp16) {
         const float sc = fp16_scale(amax);
         if (sc > 0.0f) {
@@ -1561,6 +1670,16 @@ static int choose_operands(cuscan_ctx *ctx, RefinedBuffers &R, const float *x, i
     }
     R.have_scale = true;
     return CUSCAN_OK;
+}
+
+// Operand format of the current fit's screens.
+static int operand_format(const RefinedBuffers &R) {
+    return R.split ? FMT_SPLIT : R.fp16 ? FMT_FP16 : FMT_BF16;
+}
+
+// Operand format a refined fit ended with: 0 bf16, 1 fp16, 2 split bf16 (-1: no screen ran).
+int refined_operand_format(const ForestBuffers &b) {
+    return b.refined.tile_pairs == 0 ? -1 : operand_format(b.refined);
 }
 
 // A operand of a screen and the outputs of the kNN threshold mode; the defaults mean the
@@ -1607,9 +1726,12 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.n_qblocks = ceil_div(P.nq, (int64_t)BM);
     P.n_chunks = ceil_div(n, 32);
     P.kblocks = L.kblocks;
+    P.nbk = L.nbk;
+    P.split = L.split;
     P.stages = L.stages;
+    P.cursor = as<unsigned long long>(R.cursor);
     float ca, cb, abs_c;
-    error_coefficients(d, L.d_pad, R.fp16, ca, cb, abs_c);
+    error_coefficients(d, L.d_pad, operand_format(R), R.fp16 ? R.amax_value * R.scale : R.amax_value, ca, cb, abs_c);
     P.c_a = ca;
     P.one_minus_cb = 1.0f - cb;
     P.abs_c = abs_c;
@@ -1645,6 +1767,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     }
     if (P.n_qblocks == 0) return CUSCAN_OK;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, 16, s));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.cursor.ptr, 0, 16, s));
     auto kernel = screen_kernel<M, MODE>;
     if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
     int64_t grid = P.n_qblocks < ctx->sm_count ? P.n_qblocks : ctx->sm_count;
@@ -1666,6 +1789,35 @@ static int read_screen_status(cuscan_ctx *ctx, RefinedBuffers &R, cudaStream_t s
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, 16, s));
     fallbacks = count;
     return CUSCAN_OK;
+}
+
+// The kNN list screen over every row in sorted positions and its exact re-rank. Rows whose
+// lists are inconclusive are listed by position in R.fallback, with the k-th exact distance
+// among their candidates in R.qthr; returns their count.
+static int knn_list_pass(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, const float *xs,
+                         const int32_t *perm, int64_t n, int d, int k, int32_t *ids, float *dist,
+                         cudaStream_t s, int &fallbacks) {
+    // 22 bounds per row half: enough that nearly every row's unseen bound clears its k-th
+    // exact distance at k <= 32 for bf16 screens (the rest go to the threshold re-screen), and
+    // each insertion shifts 22 registers; 20 and 24 entries measured slower
+    constexpr int M = KNN_LIST;
+    if (int rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s)) return rc;
+    for (cudaEvent_t &e : R.screen_ev)
+        if (!e) CUSCAN_CUDA(ctx, cudaEventCreate(&e));
+    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[0], s));
+    if (int rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))
+        return rc;
+    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[1], s));
+    R.screen_timed = true;
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+    const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
+    if (int rc = allow_dynamic_smem(ctx, rerank_knn_kernel<M>, rr_smem)) return rc;
+    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
+                  32 * RERANK_WARPS, rr_smem, s, xs, perm, n, d,
+                  k, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
+                  as<int32_t>(R.fallback), as<float>(R.qthr), as<int>(R.count));
+    CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
+    return read_screen_status(ctx, R, s, fallbacks);
 }
 
 int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d, int k,
@@ -1703,29 +1855,29 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
     const float *xs = as<float>(b.xp);
     const int32_t *perm = as<int32_t>(b.perm);
     // 3. screen + exact re-rank in sorted positions, outputs in original rows
-    if ((rc = prep(ctx, R, L, xs, n, d, nullptr, nullptr, s))) return rc;
-    // 22 bounds per row half: enough that nearly every row's unseen bound clears its k-th
-    // exact distance at k <= 32 for bf16 screens (the rest go to the threshold re-screen), and
-    // each insertion shifts 22 registers; 20 and 24 entries measured slower
-    constexpr int M = KNN_LIST;
-    for (cudaEvent_t &e : R.screen_ev)
-        if (!e) CUSCAN_CUDA(ctx, cudaEventCreate(&e));
-    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[0], s));
-    if ((rc = run_screen<M, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s))) return rc;
-    CUSCAN_CUDA(ctx, cudaEventRecord(R.screen_ev[1], s));
-    R.screen_timed = true;
-    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
-    if ((rc = allow_dynamic_smem(ctx, rerank_knn_kernel<M>, rr_smem))) return rc;
-    CUSCAN_KERNEL(rerank_knn_kernel<M>, (unsigned)ceil_div(n, (int64_t)RERANK_WARPS),
-                  32 * RERANK_WARPS, rr_smem, s, xs, perm, n, d,
-                  k, as<int32_t>(R.cand_ids), as<float>(R.cand_lb), ids, dist,
-                  as<int32_t>(R.fallback), as<float>(R.qthr), as<int>(R.count));
-    CUSCAN_LAUNCH(ctx, "rerank_knn_kernel");
     int fallbacks = 0;
-    if ((rc = read_screen_status(ctx, R, s, fallbacks))) return rc;
+    if ((rc = knn_list_pass(ctx, R, L, xs, perm, n, d, k, ids, dist, s, fallbacks))) return rc;
     if (refined_rows) *refined_rows += n;
+    if (!R.fp16 && !R.split && (double)fallbacks > TIGHTEN_TRIGGER * (double)n) {
+        // the bf16 bound is too loose for this data (norms large against the neighbour
+        // distances): screen again, and run the Borůvka rounds, with split-bf16 operands, or
+        // with scaled fp16 operands where a split tile does not fit the pipeline
+        Layout Ls;
+        const float sc = fp16_scale(R.amax_value);
+        if (refined_layout(n, d, Ls, true)) {
+            R.split = true;
+            L = Ls;
+        } else if (sc > 0.0f) {
+            R.fp16 = true;
+            R.scale = sc;
+        }
+        if (R.split || R.fp16)
+            if ((rc = knn_list_pass(ctx, R, L, xs, perm, n, d, k, ids, dist, s, fallbacks)))
+                return rc;
+    }
     if (fallbacks == 0) return CUSCAN_OK;
+    constexpr int M = KNN_LIST;
+    const size_t rr_smem = sizeof(float) * RERANK_WARPS * (size_t)rerank_warp_floats(d);
     int32_t *exact_rows = as<int32_t>(R.fallback);
     int exact = fallbacks;
     if (fallbacks >= RESCREEN_MIN_ROWS && k <= 2 * KNN_CAP) {
@@ -1733,7 +1885,7 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
         // not exceed the row's k-th distance among its candidates is appended and re-ranked
         const int64_t nq = fallbacks;
         const int64_t nq_pad = ceil_div(nq, (int64_t)BN) * BN;
-        rc = ensure(ctx, R.xq, (size_t)nq_pad * L.d_pad * 2, "re-screen tiles");
+        rc = ensure(ctx, R.xq, (size_t)(nq_pad / BN) * L.nbk * KBLOCK_B, "re-screen tiles");
         if (!rc) rc = ensure(ctx, R.pq, sizeof(float) * nq_pad, "re-screen norms");
         if (!rc) rc = ensure(ctx, R.mq, sizeof(float) * nq_pad, "re-screen norms");
         if (!rc) rc = ensure(ctx, R.cand2, sizeof(int32_t) * nq * 2 * KNN_CAP, "re-screen candidates");
@@ -1792,7 +1944,7 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
         return launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s);
     RefinedBuffers &R = b.refined;
     Layout L;
-    refined_layout(n, d, L);
+    refined_layout(n, d, L, R.split != 0);
     int rc = choose_operands(ctx, R, xp, n, d, s);
     if (rc) return rc;
     if (!R.range_ok)  // values large enough to overflow f32: the exact round decides alone
@@ -1855,7 +2007,7 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     if (subset) {
         nq = active;
         const int64_t nq_pad = ceil_div(nq > 0 ? nq : 1, (int64_t)BN) * BN;
-        rc = ensure(ctx, R.xq, (size_t)nq_pad * L.d_pad * 2, "subset tiles");
+        rc = ensure(ctx, R.xq, (size_t)(nq_pad / BN) * L.nbk * KBLOCK_B, "subset tiles");
         if (!rc) rc = ensure(ctx, R.pq, sizeof(float) * nq_pad, "subset norms");
         if (!rc) rc = ensure(ctx, R.mq, sizeof(float) * nq_pad, "subset norms");
         if (rc) return rc;
@@ -1909,31 +2061,55 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
     return CUSCAN_OK;
 }
 
+// The per-row terms of the bound for the debug entry point: (ps, pb, cm, m) with
+// ps = (1 - C_B) p - abs_c, pb = (1 - C_B) p, cm = C_A m, so that the screen's bound of entry
+// (r, c) is fmaf(-cm_r, m_c, fmaf(-2, acc_rc, pb_c) + ps_r) (screen units).
+__global__ void debug_rows_kernel(const float *__restrict__ pnorm, const float *__restrict__ mnorm,
+                                  int64_t n, float one_minus_cb, float abs_c, float c_a,
+                                  float *__restrict__ rows) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float p = pnorm[r], m = mnorm[r];
+    rows[4 * r + 0] = one_minus_cb * p - abs_c;
+    rows[4 * r + 1] = one_minus_cb * p;
+    rows[4 * r + 2] = c_a * m;
+    rows[4 * r + 3] = m;
+}
+
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      int operands, float *out, float *scale_out, cudaStream_t s) {
-    Layout L;
-    if (!refined_layout(n, d, L))
-        return fail(ctx, CUSCAN_CAPACITY, "shape outside the tensor-core tiling");
+                      int operands, float *out, float *rows_out, float *scale_out,
+                      cudaStream_t s) {
     RefinedBuffers &R = b.refined;
     R.have_scale = false;
-    R.want_fp16 = operands == 1;
-    int rc = CUSCAN_OK;
-    if (operands == 1) {
-        // fp16 of x * scale with the fit's own power-of-two scale
-        if ((rc = choose_operands(ctx, R, x, n, d, s))) return rc;
-        if (!R.fp16) return fail(ctx, CUSCAN_INVALID_INPUT, "no fp16 scale for this data");
-    } else {
-        R.fp16 = false;  // the raw accumulator of bf16 operands
-        R.scale = 1.0f;
-    }
-    if (scale_out) *scale_out = R.scale;
-    R.have_scale = false;
+    R.want_fp16 = operands == FMT_FP16;
+    int rc = choose_operands(ctx, R, x, n, d, s);
+    if (rc) return rc;
+    if (operands == FMT_FP16 && !R.fp16)
+        return fail(ctx, CUSCAN_INVALID_INPUT, "no fp16 scale for this data");
+    R.split = operands == FMT_SPLIT;
+    Layout L;
+    if (!refined_layout(n, d, L, R.split))
+        return fail(ctx, CUSCAN_CAPACITY, "shape outside the tensor-core tiling%s",
+                    R.split ? " (split copies need d <= 64)" : "");
+    if (scale_out) *scale_out = R.fp16 ? R.scale : 1.0f;
     rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
     if (!rc) rc = run_screen<32, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
-    if (rc) return rc;
-    int fallbacks = 0;
-    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
-    return read_screen_status(ctx, R, s, fallbacks);
+    if (!rc && rows_out) {
+        float ca, cb, abs_c;
+        error_coefficients(d, L.d_pad, operand_format(R), R.fp16 ? R.amax_value * R.scale : R.amax_value, ca, cb, abs_c);
+        CUSCAN_KERNEL(debug_rows_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, as<float>(R.pnorm),
+                      as<float>(R.mnorm), n, 1.0f - cb, abs_c, ca, rows_out);
+        CUSCAN_LAUNCH(ctx, "debug_rows_kernel");
+    }
+    if (!rc) {
+        int fallbacks = 0;
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
+        rc = read_screen_status(ctx, R, s, fallbacks);
+    }
+    R.have_scale = false;
+    R.split = false;
+    R.fp16 = false;
+    return rc;
 }
 
 }  // namespace cuscan

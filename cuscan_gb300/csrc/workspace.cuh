@@ -20,6 +20,14 @@ struct FitWorkspace {
     DevStatus *host_status = nullptr;              // pinned
     cudaEvent_t ev[6] = {};
     PackWorkspace *pack = nullptr;                 // created by the first packed call
+    // per Borůvka round of the last fit: query rows screened, tensor-core tiles run, candidate
+    // kernel time (ms), ordered cross-component pairs entering the round
+    static constexpr int kMaxRoundLog = 64;
+    int round_count = 0;
+    int64_t round_rows[kMaxRoundLog] = {};
+    int64_t round_tiles[kMaxRoundLog] = {};
+    double round_ms[kMaxRoundLog] = {};
+    double round_cross[kMaxRoundLog] = {};
 };
 constexpr int kOwnBufferCount = 17;
 

@@ -93,6 +93,10 @@ typedef struct cuscan_fit_stats {
     double knn_screen_ms;    /* the kNN tensor-core screen launch alone (0 when the fit ran
                                 the exact kernels only) */
     int64_t symmetric_rounds; /* Borůvka rounds screened with each unordered pair once */
+    int64_t operand_format;   /* screen operands the fit ended with: 0 bf16, 1 fp16 (scaled),
+                                 2 split bf16 (hi + lo). A bf16-refined fit whose plain bf16
+                                 bound leaves too many kNN rows inconclusive switches to split
+                                 bf16 (d <= 64) or scaled fp16 (wider rows); -1: no screen ran */
 } cuscan_fit_stats;
 
 /* ---- context ---- */
@@ -238,6 +242,52 @@ typedef struct cuscan_fit_item {
 int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, int32_t count);
 
 /*
+ * Per Borůvka round of the context's last fit (no reference counterpart; the reference logs
+ * the component counts of its rounds only): the query rows the round screened (all n for the
+ * plain f32 form), the 128 x 256 tensor-core tiles its screens ran, its candidate-kernel time
+ * in ms and the ordered cross-component pairs entering it. Fills at most max_rounds entries of
+ * each non-null array and returns the number of rounds (-1 on a null context).
+ */
+int cuscan_fit_round_stats(const cuscan_ctx *ctx, int32_t max_rounds, int64_t *rows,
+                           int64_t *tiles, double *ms, double *cross_pairs);
+
+/*
+ * Row shards: one fit split by query rows over ranks (processes, one per GPU), each holding
+ * every point. A rank computes the kNN rows and the Borůvka candidates of its own rows
+ * [row_begin, row_end); the ranks exchange results on the host and every rank merges the same
+ * rounds, so all ranks hold the same forest. The reference runs these steps on one device in
+ * HDBSCAN::spanning_tree (crates/hdbscan/src/estimator.rs:689-874) with the per-row rule of
+ * crates/hdbscan/src/kernels/boruvka.rs:68-140 over row blocks (boruvka.rs:28-66,147-288).
+ *  1. kNN rows of the shard: cuscan_exact_knn with query = data + row_begin * d, nq = the
+ *     shard's rows, query_offset = row_begin; then an all-gather of the rows.
+ *  2. cuscan_shard_seed: core distances and the kNN seed forest (mst.rs:368-420) from the full
+ *     kNN rows; labels[n] receive each point's component (its smallest point), mst_* the seed
+ *     edges; returns the edge and component counts.
+ *  3. Each round, cuscan_shard_round_keys: row_keys[n] receive, for the shard's rows,
+ *     (canonical weight bits << 32) | destination of the row's cheapest cross-component edge,
+ *     and ~0 elsewhere; an all-reduce MIN over the ranks' arrays gives every row's key (keys
+ *     of non-negative weights are below 2^63, so they order alike as signed integers).
+ *  4. cuscan_shard_round_merge: the reduced keys merged exactly as a fit core round (winners,
+ *     cycle breaking, emit in merge order, union); mst_* receive the round's edges after the
+ *     earlier ones; once one component remains and mst_weight is non-null, it receives the f64
+ *     total weight. Repeat 3-4 until one component remains.
+ * All pointers are device pointers; data, core_sq and labels are the full arrays in original
+ * row order. No counterpart in the reference's surface, which has no multi-device path.
+ */
+int cuscan_shard_seed(cuscan_ctx *ctx, int64_t n, int32_t d, int32_t min_samples,
+                      const int32_t *knn_ids, const float *knn_sq, float *core_sq,
+                      int32_t *labels, uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                      int64_t *n_edges, int64_t *components, void *stream);
+int cuscan_shard_round_keys(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                            const int32_t *labels, int64_t n, int32_t d, int64_t row_begin,
+                            int64_t row_end, uint64_t *row_keys, void *stream);
+int cuscan_shard_round_merge(cuscan_ctx *ctx, const float *data, const float *core_sq,
+                             int32_t *labels, int64_t n, int32_t d, const uint64_t *row_keys,
+                             uint32_t *mst_src, uint32_t *mst_dst, float *mst_wsq,
+                             int64_t *n_edges, int64_t *components, double *mst_weight,
+                             void *stream);
+
+/*
  * Diagnostic of the bf16 tensor-core screen (no reference counterpart): runs the screening
  * pipeline on `data` (device, n >= 256 rows) and writes the raw fp32 accumulator of the first
  * 128-row query block against the first 256-row reference tile, i.e. the bf16 dot products
@@ -248,11 +298,15 @@ int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int3
 /*
  * The same diagnostic for a chosen operand format: operands 0 = bf16 (as above), 1 = fp16 of
  * x * scale with the power-of-two scale the fp16-refined fits choose for this data (written to
- * *scale_out when given; the accumulator is then scale^2 times the dot products).
+ * *scale_out when given; the accumulator is then scale^2 times the dot products), 2 = split
+ * bf16 (hi.hi' + hi.lo' + lo.hi', d <= 64). With rows_out (device, float[n][4]) every row's
+ * bound terms (ps, pb, cm, m) are written, ps = (1 - C_B) p - abs_c, pb = (1 - C_B) p,
+ * cm = C_A m, so that the screen's lower bound of entry (r, c) is
+ * fmaf(-cm_r, m_c, fmaf(-2, tile[r][c], pb_c) + ps_r), in screen units.
  */
 int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
-                                      int32_t operands, float *tile_out, float *scale_out,
-                                      void *stream);
+                                      int32_t operands, float *tile_out, float *rows_out,
+                                      float *scale_out, void *stream);
 
 /* ---- host-side extraction (no device work) ---- */
 

@@ -210,15 +210,42 @@ def test_refined_vmf_matches_oracle_and_uses_tensor_screen(gpu_ctx):
 
 
 @pytest.mark.parametrize("precision", [_lib.PRECISION_BF16_REFINED, _lib.PRECISION_FP16_REFINED])
-def test_threshold_rescreen_matches_oracle(gpu_ctx, precision):
-    """Gaussian blobs far from the origin (centres in [-10, 10]^64, std 0.5-2): the first kNN
-    screen leaves hundreds of rows inconclusive, which the threshold re-screen resolves; the
-    result equals the oracle bit for bit."""
+def test_far_blobs_match_oracle(gpu_ctx, precision):
+    """Gaussian blobs far from the origin (centres in [-10, 10]^64, std 0.5-2): norms are large
+    against the neighbour distances. The plain bf16 bound leaves most kNN rows inconclusive, so
+    the bf16-refined fit screens again with split-bf16 operands and keeps them for its rounds;
+    the fp16 screen leaves hundreds of rows to the threshold re-screen. Both equal the oracle
+    bit for bit."""
     x = synthetic.gaussian_mixture(20000, 64, 25, seed=20064)
     got = gpu_ctx.fit_core(x, 5, precision)
-    assert got["stats"]["rescreened_rows"] >= 256
-    assert got["stats"]["fallback_rows"] < got["stats"]["rescreened_rows"]
+    if precision == _lib.PRECISION_BF16_REFINED:
+        assert got["stats"]["operand_format"] == 2
+    else:
+        assert got["stats"]["operand_format"] == 1
+        assert got["stats"]["rescreened_rows"] >= 256
+        assert got["stats"]["fallback_rows"] < got["stats"]["rescreened_rows"]
     assert_fit_equal(got, O.fit_core(x, 5))
+
+
+def test_wide_far_blobs_tighten_to_fp16_and_match_oracle(gpu_ctx):
+    """The same kind of data at d = 128, where a split tile does not fit the pipeline: the
+    bf16-refined fit tightens to scaled fp16 operands and equals the oracle bit for bit."""
+    x = synthetic.gaussian_mixture(12000, 128, 20, seed=12128)
+    got = gpu_ctx.fit_core(x, 5, _lib.PRECISION_BF16_REFINED)
+    assert got["stats"]["operand_format"] == 1
+    assert_fit_equal(got, O.fit_core(x, 5))
+
+
+def test_bf16_threshold_rescreen_matches_oracle(gpu_ctx):
+    """vMF-like unit vectors (n = 60,000, d = 128, min_samples 15, the headline workload's
+    kind): the bf16 list screen leaves a small share of rows inconclusive (too few to tighten
+    the operands), which the bf16 threshold re-screen resolves; the result equals the oracle
+    bit for bit."""
+    x = synthetic.vmf_like(n=60000, d=128, clusters=60, seed=60128)
+    got = gpu_ctx.fit_core(x, 15, _lib.PRECISION_BF16_REFINED)
+    assert got["stats"]["operand_format"] == 0
+    assert got["stats"]["rescreened_rows"] >= 256
+    assert_fit_equal(got, O.fit_core(x, 15))
 
 
 def test_full_size_refined_equals_plain(gpu_ctx):
