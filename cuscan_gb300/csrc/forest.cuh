@@ -29,10 +29,10 @@ struct RefinedBuffers {
     Buffer urow, colcnt, colbuf;  // symmetric Borůvka: row bounds, column-side buffers
     Buffer act_flag, act_idx, act_pos;  // Borůvka rows that can hold their component's edge
     Buffer rowlb, lbtmp;  // lower bounds of each row's cheapest cross edge (original order)
-    Buffer cursor;        // tiles issued by the CTAs of the running screen (shared tile order)
     // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
     bool want_fp16 = false;  // requested by the caller's precision
     bool fp16 = false;       // in use (the data's range allows a scale)
+    Buffer cursor;        // tiles issued by the CTAs of the running kNN screen
     bool split = false;      // split-bf16 operands (hi + lo) in use for the current fit
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;

@@ -55,8 +55,7 @@ struct Params {
     const uint8_t *xt;        // 16-bit tiles, pre-swizzled (see tile_16bit_kernel)
     int nbk;                  // K blocks per tile row of the copy: kblocks, or 2 kblocks (split)
     int split;                // split bf16: blocks [0, kblocks) hold hi, [kblocks, 2 kblocks) lo
-    // tiles issued by all CTAs so far: a query block starts its sweep of the shared tile order
-    // where the other CTAs are, so that the tiles they stream stay in L2
+    // kNN sweeps: tiles issued by all CTAs so far (see knn_tile)
     unsigned long long *cursor;
     const float *pnorm;       // [n_pad] f32 squared norms (+inf on padding rows)
     const float *mnorm;       // [n_pad] norms rounded up (0 on padding rows)
@@ -342,12 +341,20 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
     }
 }
 
-// Order in which query block qb visits the reference tiles: first a window of WARM tiles around
-// the block's own tile (in cell-sorted data these hold the block's nearest neighbours, so the
-// per-row thresholds tighten at once), then every other tile in one cyclic order shared by all
-// CTAs, entered at the rotation `rot` the producer chose when the block started: where the
-// CTAs are on average, so that blocks that start at different times still stream the same
-// tiles and share them in L2.
+// Order in which query block qb visits the reference tiles. Every order starts with a window of
+// WARM tiles around the block's own tile: in cell-sorted data these hold the block's nearest
+// neighbours, so the per-row thresholds tighten at once.
+//
+// Borůvka rounds (tile_order) go on cyclically from the window. Their blocks skip different
+// tiles, and the tiles they run stay in L2 anyway (one to two GB of DRAM reads per round at
+// 500,000 points), so the cheapest order wins there.
+//
+// The kNN sweeps (knn_tile) run every tile for every block. After the window a block enters one
+// cyclic order of the other tiles that all CTAs share, at the rotation `rot` the producer takes
+// from the tile cursor when the block starts: the average position of the CTAs. Blocks started
+// at different times then stream the same tiles and share them in L2. Without the rotation the
+// CTAs drift apart over the waves of the persistent loop and the sweep reads the copy from
+// DRAM about a thousand times over.
 constexpr int64_t WARM = 4;
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float r;
@@ -390,12 +397,16 @@ __device__ __forceinline__ int64_t window_start(const Params &P, int64_t qb) {
     if (a > P.n_tiles - w) a = P.n_tiles - w;
     return a;
 }
-__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_t rot, int64_t i) {
-    const int64_t w = P.n_tiles < WARM ? P.n_tiles : WARM;
+__device__ __forceinline__ int64_t tile_order(const Params &P, int64_t a, int64_t i) {
+    const int64_t t = a + i;
+    return t < P.n_tiles ? t : t - P.n_tiles;
+}
+// n tiles, window [a, a + w), rotation r < n - w (r = 0 when n <= WARM).
+__device__ __forceinline__ int32_t knn_tile(int32_t n, int32_t a, int32_t r, int32_t i) {
+    const int32_t w = n < (int32_t)WARM ? n : (int32_t)WARM;
     if (i < w) return a + i;
-    const int64_t rest = P.n_tiles - w;  // > 0 here; rot < rest
-    int64_t j = i - w + rot;
-    if (j >= rest) j -= rest;
+    int32_t j = i - w + r;
+    if (j >= n - w) j -= n - w;
     return j < a ? j : j + w;
 }
 
@@ -407,9 +418,8 @@ __device__ __forceinline__ int64_t vis_count(const Params &P, int64_t qb) {
     return SYM ? P.n_tiles - (qb >> 1) : P.n_tiles;
 }
 template <bool SYM>
-__device__ __forceinline__ int64_t vis_tile(const Params &P, int64_t qb, int64_t wa,
-                                            int64_t rot, int64_t i) {
-    return SYM ? (qb >> 1) + i : tile_order(P, wa, rot, i);
+__device__ __forceinline__ int64_t vis_tile(const Params &P, int64_t qb, int64_t wa, int64_t i) {
+    return SYM ? (qb >> 1) + i : tile_order(P, wa, i);
 }
 
 // The query block a CTA takes at its qi-th step (blocks in order, strided over the CTAs).
@@ -464,6 +474,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     constexpr bool SYM = MODE == MODE_BORUVKA_SYM;
     constexpr bool THRESH = MODE == MODE_KNN_THRESHOLD;
     constexpr bool APPEND = BORUVKA || THRESH;  // threshold modes append to per-row buffers
+    constexpr bool ROT = !BORUVKA;              // kNN sweeps: rotated shared tile order
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t a_bytes = (uint32_t)P.nbk * KBLOCK_A;
@@ -480,11 +491,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     uint64_t *t_full = a_full + 2;   // [2]
     uint64_t *t_empty = a_full + 4;  // [2]
     uint64_t *done = a_full + 6;     // MMA drain on the abort path
-    uint64_t *rot_full = a_full + 7;    // [4]: the producer published a block's rotation
-    uint64_t *rot_empty = a_full + 11;  // [4]: every epilogue warp has read it
+    uint64_t *rot_full = a_full + 7;    // [4] kNN sweeps: the producer published a rotation
+    uint64_t *rot_empty = a_full + 11;  // [4] every epilogue warp has read it
     uint32_t *tmem_slot = (uint32_t *)(a_full + 15);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
-    int64_t *rot_val = (int64_t *)(tmem_slot + 2);  // [4]
+    int32_t *rot_val = (int32_t *)(tmem_slot + 2);  // [4]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -537,23 +548,26 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                                       (uint64_t)(qb & 1) * KBLOCK_A;
                 for (int kb = 0; kb < P.nbk; ++kb)
                     bulk_g2s(sA + kb * KBLOCK_A, asrc + (uint64_t)kb * KBLOCK_B, KBLOCK_A, a_full);
-                // this block's rotation of the shared tile order: the average position of the
-                // CTAs (tiles issued so far over the grid), published to the epilogue warps
-                int64_t rot = 0;
-                if (!SYM && P.n_tiles > WARM) {
-                    const unsigned long long all = *(volatile unsigned long long *)P.cursor;
-                    rot = (int64_t)((all / gridDim.x) % (unsigned long long)(P.n_tiles - WARM));
-                }
-                const uint32_t rs = li & 3;
-                if (!mbar_wait(&rot_empty[rs], ((li >> 2) & 1) ^ 1, abort, P.error)) break;
-                rot_val[rs] = rot;
-                mbar_arrive(&rot_full[rs]);
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
+                // kNN sweeps: the block's rotation of the shared order (the CTAs' average
+                // position: tiles issued so far over the grid), published to the epilogue warps
+                int32_t rot = 0;
+                if (ROT) {
+                    if (P.n_tiles > WARM) {
+                        const unsigned long long all = *(volatile unsigned long long *)P.cursor;
+                        rot = (int32_t)((all / gridDim.x) % (unsigned long long)(P.n_tiles - WARM));
+                    }
+                    const uint32_t rs = li & 3;
+                    if (!mbar_wait(&rot_empty[rs], ((li >> 2) & 1) ^ 1, abort, P.error)) break;
+                    rot_val[rs] = rot;
+                    mbar_arrive(&rot_full[rs]);
+                }
                 for (int64_t i = 0; i < nvis; ++i) {
-                    const int64_t t = vis_tile<SYM>(P, qb, wa, rot, i);
+                    const int64_t t = ROT ? (int64_t)knn_tile((int32_t)P.n_tiles, (int32_t)wa, rot, (int32_t)i)
+                                          : vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     if (!mbar_wait(&empty[stage], phase ^ 1, abort, P.error)) break;
                     issued[stage] = 2u | phase;
@@ -567,7 +581,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                         stage = 0;
                         phase ^= 1;
                     }
-                    atomicAdd(P.cursor, 1ull);
+                    if (ROT) atomicAdd(P.cursor, 1ull);
                 }
             }
             if (*abort) {
@@ -596,13 +610,11 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 int32_t qlo = 0, qhi = 0;
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
-                // the set of tiles the block runs does not depend on their order: visit them in
-                // the unrotated order to count the skipped ones
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
                 bool ok = true;
                 for (int64_t i = 0; i < nvis; ++i) {
-                    const int64_t t = vis_tile<SYM>(P, qb, wa, 0, i);
+                    const int64_t t = vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                     if (!mbar_wait(&t_empty[b], tp ^ 1, abort, P.error)) { ok = false; break; }
@@ -666,14 +678,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         uint32_t tcount = 0;
         for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
             const int64_t qb = block_at<SYM>(P, qi);
-            // the block's rotation of the tile order, published by the producer (li: this
-            // CTA's query step)
-            const uint32_t li = (uint32_t)((qi - blockIdx.x) / gridDim.x);
-            const uint32_t rs = li & 3;
-            if (!mbar_wait(&rot_full[rs], (li >> 2) & 1, abort, P.error)) break;
-            const int32_t rot = (int32_t)*(volatile int64_t *)&rot_val[rs];
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&rot_empty[rs]);
+            // kNN sweeps: the block's rotation, published by the producer (li: this CTA's query
+            // step)
+            int32_t rot = 0;
+            if (ROT) {
+                const uint32_t li = (uint32_t)((qi - blockIdx.x) / gridDim.x);
+                const uint32_t rs = li & 3;
+                if (!mbar_wait(&rot_full[rs], (li >> 2) & 1, abort, P.error)) break;
+                rot = *(volatile int32_t *)&rot_val[rs];
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&rot_empty[rs]);
+            }
             const int64_t row = qb * BM + row_local;  // query row
             const bool valid = row < P.nq;
             const int64_t self = valid && P.qpos ? (int64_t)P.qpos[row] : row;
@@ -717,9 +732,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 cmmax_w = warp_max_f(valid ? cm_i : 0.0f);
                 coremin_w = warp_min_f(valid ? core_i : CUSCAN_INF);
             }
-            // next visited position i (>= i0) in this block's tile order
+            auto tile_at = [&](int64_t i) -> int64_t {
+                return ROT ? (int64_t)knn_tile((int32_t)P.n_tiles, (int32_t)wa, rot, (int32_t)i)
+                           : vis_tile<SYM>(P, qb, wa, i);
+            };
+            // next visited position i (>= i0) in this block's tile order, and its tile t_at
+            int64_t t_at = 0;
             auto next_index = [&](int64_t i) -> int64_t {
-                while (i < nvis && tile_skipped<BORUVKA>(P, vis_tile<SYM>(P, qb, wa, rot, i), qlo, qhi)) ++i;
+                for (; i < nvis; ++i) {
+                    t_at = tile_at(i);
+                    if (!tile_skipped<BORUVKA>(P, t_at, qlo, qhi)) break;
+                }
                 return i;
             };
             // per-tile column data, fetched one tile ahead
@@ -758,10 +781,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
             };
             int64_t ti = next_index(0);
-            if (ti < nvis) prefetch(vis_tile<SYM>(P, qb, wa, rot, ti));
+            if (ti < nvis) prefetch(t_at);
             bool ok = true;
             while (ti < nvis) {
-                const int64_t t = vis_tile<SYM>(P, qb, wa, rot, ti);
+                const int64_t t = t_at;
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
                 float *pb = my_pb + b * HALF;
@@ -809,7 +832,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
-                if (ti_next < nvis) prefetch(vis_tile<SYM>(P, qb, wa, rot, ti_next));
+                if (ti_next < nvis) prefetch(t_at);
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -1129,17 +1152,6 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem_base)
                      : "memory");
     }
-}
-
-// Exact f32 squared distance in the reference's order.
-__device__ __forceinline__ float exact_d2(const float *__restrict__ a, const float *__restrict__ b,
-                                          int d) {
-    float acc = 0.0f;
-    for (int f = 0; f < d; ++f) {
-        const float t = a[f] - b[f];
-        acc = __fmaf_rn(t, t, acc);
-    }
-    return acc;
 }
 
 // Exact squared distance (the reference's order) from the warp's query row q_s (shared) to the

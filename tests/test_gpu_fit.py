@@ -236,24 +236,18 @@ def test_wide_far_blobs_tighten_to_fp16_and_match_oracle(gpu_ctx):
     assert_fit_equal(got, O.fit_core(x, 5))
 
 
-def test_bf16_threshold_rescreen_matches_oracle(gpu_ctx):
-    """vMF-like unit vectors (n = 60,000, d = 128, min_samples 15, the headline workload's
-    kind): the bf16 list screen leaves a small share of rows inconclusive (too few to tighten
-    the operands), which the bf16 threshold re-screen resolves; the result equals the oracle
-    bit for bit."""
-    x = synthetic.vmf_like(n=60000, d=128, clusters=60, seed=60128)
-    got = gpu_ctx.fit_core(x, 15, _lib.PRECISION_BF16_REFINED)
-    assert got["stats"]["operand_format"] == 0
-    assert got["stats"]["rescreened_rows"] >= 256
-    assert_fit_equal(got, O.fit_core(x, 15))
-
-
 def test_full_size_refined_equals_plain(gpu_ctx):
     """vmf_500k_d128 reduced to n=150000 (large enough for the symmetric Borůvka screen):
     bf16-refined and plain fits agree bit for bit."""
     x, ms, _ = synthetic.workload("vmf_500k_d128", n=150000)
     a = gpu_ctx.fit_core(x, ms, _lib.PRECISION_PLAIN)
     b = gpu_ctx.fit_core(x, ms, _lib.PRECISION_BF16_REFINED)
+    # the headline kind of data keeps bf16 operands; the rows its lists leave inconclusive go
+    # through the bf16 threshold re-screen
+    print(f"[vmf 150k] rescreened {b['stats']['rescreened_rows']}, "
+          f"exact {b['stats']['fallback_rows']}")
+    assert b["stats"]["operand_format"] == 0
+    assert b["stats"]["rescreened_rows"] >= 256
     for key in ("knn_ids", "src", "dst"):
         np.testing.assert_array_equal(a[key], b[key])
     for key in ("knn_sq", "core_sq", "wsq"):
