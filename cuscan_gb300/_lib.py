@@ -52,7 +52,7 @@ SIGNATURES = {
     "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_debug_screen_tile_operands": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32,
-                                                    _VP, _VP, C.POINTER(C.c_float), _VP]),
+                                                    _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
     "cuscan_fit_round_stats": (C.c_int, [_VP, C.c_int32, _VP, _VP, _VP, _VP]),
     "cuscan_shard_seed": (C.c_int, [_VP, C.c_int64, C.c_int32, C.c_int32, _VP, _VP, _VP, _VP,
                                     _VP, _VP, _VP, C.POINTER(C.c_int64),
@@ -357,18 +357,21 @@ class Context:
                                                     dst, wsq, C.byref(m), C.byref(stats), stream))
         return int(m.value), stats
 
-    def debug_screen_tile(self, data, n, d, tile_out, stream=None, operands=None, rows_out=None):
+    def debug_screen_tile(self, data, n, d, tile_out, stream=None, operands=None, rows_out=None,
+                          chunk_out=None):
         """Raw accumulator of the first 128 x 256 screen tile; with `operands` (0 bf16, 1 fp16,
         2 split bf16) the chosen format, returning the operand scale (the tile holds scale^2 x
         the dots). rows_out (device float[n][4]) receives every row's bound terms
-        (ps, pb, cm, m)."""
-        if operands is None:
+        (ps, pb, cm, m); chunk_out (device float[128][8]) the screen's maxima of the tile's
+        32-column chunks."""
+        if operands is None and chunk_out is None:
             self.check(self._lib.cuscan_debug_screen_tile(self.handle, data, n, d, tile_out,
                                                           stream))
             return 1.0
         scale = C.c_float(0.0)
         self.check(self._lib.cuscan_debug_screen_tile_operands(
-            self.handle, data, n, d, operands, tile_out, rows_out, C.byref(scale), stream))
+            self.handle, data, n, d, operands or 0, tile_out, rows_out, chunk_out, C.byref(scale),
+            stream))
         return float(scale.value)
 
     def round_stats(self) -> list[dict]:

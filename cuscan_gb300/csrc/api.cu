@@ -19,8 +19,8 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                               const float *core, const int32_t *label, cudaStream_t s,
                               int64_t *fallback_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      int operands, float *out, float *rows_out, float *scale_out,
-                      cudaStream_t s);
+                      int operands, float *out, float *rows_out, float *chunk_out,
+                      float *scale_out, cudaStream_t s);
 int refined_operand_format(const ForestBuffers &b);
 size_t refined_workspace_bytes(int64_t n, int d, int k);
 
@@ -518,7 +518,7 @@ int cuscan_shard_round_merge(cuscan_ctx *ctx, const float *data, const float *co
 
 int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
                                       int32_t operands, float *tile_out, float *rows_out,
-                                      float *scale_out, void *stream) {
+                                      float *chunk_out, float *scale_out, void *stream) {
     if (!ctx) return CUSCAN_INVALID_INPUT;
     clear_error(ctx);
     if (n < 256 || d <= 0 || !data || !tile_out)
@@ -530,13 +530,13 @@ int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_
     int rc = forest_reserve(ctx, ctx->fit->forest, n, d);
     if (rc) return rc;
     return debug_screen_tile(ctx, ctx->fit->forest, data, n, d, operands, tile_out, rows_out,
-                             scale_out, s);
+                             chunk_out, scale_out, s);
 }
 
 int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
                              float *tile_out, void *stream) {
     return cuscan_debug_screen_tile_operands(ctx, data, n, d, 0, tile_out, nullptr, nullptr,
-                                             stream);
+                                             nullptr, stream);
 }
 
 }  // extern "C"

@@ -583,7 +583,7 @@ int forest_buffers(ForestBuffers &b, Buffer **out) {
                      &r.cbound, &r.rowcnt, &r.pivots, &r.cells, &r.cell_d, &r.absmax,
                      &r.qthr, &r.xq, &r.pq, &r.mq, &r.cand2, &r.rowcnt2, &r.fallback2,
                      &r.urow, &r.colcnt, &r.colbuf, &r.act_flag, &r.act_idx, &r.act_pos,
-                     &r.rowlb, &r.lbtmp, &r.cursor};
+                     &r.rowlb, &r.lbtmp, &r.cursor, &r.colp, &r.colc, &r.cmin};
     static_assert(sizeof(all) / sizeof(all[0]) == kForestBufferCount, "buffer list");
     const int count = (int)(sizeof(all) / sizeof(all[0]));
     if (out)

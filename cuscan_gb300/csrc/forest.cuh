@@ -32,7 +32,8 @@ struct RefinedBuffers {
     // operand format of the current fit: fp16 of x * scale (scale a power of two), or bf16
     bool want_fp16 = false;  // requested by the caller's precision
     bool fp16 = false;       // in use (the data's range allows a scale)
-    Buffer cursor;        // tiles issued by the CTAs of the running kNN screen
+    Buffer cursor;        // kNN screens: tiles issued, query blocks taken
+    Buffer colp, colc, cmin;  // column terms of the running screen (screen_columns_kernel)
     bool split = false;      // split-bf16 operands (hi + lo) in use for the current fit
     bool have_scale = false; // scale computed for the current fit
     float scale = 1.0f;
@@ -65,7 +66,7 @@ struct ForestBuffers {
 int forest_reserve(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d);
 void forest_release(ForestBuffers &b);
 // Every device buffer of the forest and of the bf16 screen (out may be null); returns the count.
-constexpr int kForestBufferCount = 61;
+constexpr int kForestBufferCount = 64;
 int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);

@@ -46,19 +46,21 @@ constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of 
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded mbarrier waits: 2 s of wall time
 constexpr uint32_t WAIT_POLLS = 1u << 22;      // poll bound of the abort-path drains
 constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
-// per epilogue warp: [2][HALF] scaled norms, [2][HALF] cores, [2][HALF] m, then [2][4] (min
-// scaled norm, min core) of each 32-column chunk
-constexpr int PB_STRIDE = 6 * HALF + 16;
 constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row half
 
 struct Params {
     const uint8_t *xt;        // 16-bit tiles, pre-swizzled (see tile_16bit_kernel)
     int nbk;                  // K blocks per tile row of the copy: kblocks, or 2 kblocks (split)
     int split;                // split bf16: blocks [0, kblocks) hold hi, [kblocks, 2 kblocks) lo
-    // kNN sweeps: tiles issued by all CTAs so far (see knn_tile)
+    // kNN sweeps: [0] tiles issued by all CTAs so far (see knn_tile), [1] query blocks taken
     unsigned long long *cursor;
     const float *pnorm;       // [n_pad] f32 squared norms (+inf on padding rows)
     const float *mnorm;       // [n_pad] norms rounded up (0 on padding rows)
+    // column terms of this launch (screen_columns_kernel): (1 - C_B) p, cores in screen units
+    // (Borůvka; 0 past n) and (min, min) of both over every 32-column chunk
+    const float *colp;
+    const float *colc;
+    const float4 *cmin;       // [n_pad / 64]: two chunks per entry
     const float *core;        // [n] core distances (Borůvka)
     const int32_t *label;     // [n] component labels (Borůvka)
     const float *tile_mmax;   // [n_tiles] max m over each 256-row tile
@@ -72,7 +74,8 @@ struct Params {
     int32_t *cand_ids;        // [n][M]
     float *cand_lb;           // [n][M]
     int *error;               // [0]: error flag; bytes 8..15: (qb, tile) pairs the MMA ran (u64)
-    float *debug_tile;        // when set: CTA 0 writes its first raw 128 x 256 accumulator tile
+    float *debug_tile;        // when set: the raw 128 x 256 accumulator of query block 0 x tile 0
+    float *debug_chunk;       // with debug_tile: [128][8] the phase-1 maxima of its 32-column chunks
     float c_b;                // norm coefficient of the bound (upper bounds use it)
     uint32_t *cbound;         // Borůvka: per-component upper bound of the cheapest edge (f32 bits)
     int32_t *rowcnt;          // Borůvka: candidates appended per row half ([n][2])
@@ -222,6 +225,23 @@ __device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t (&r)[32
           "=r"(r[31])
         : "r"(taddr));
 }
+// Issue a 32-column TMEM load that also returns the largest of the 32 values (tcgen05.ld.red,
+// sm_103a): the reduction rides on the load, so the chunk maxima of the screens cost no ALU
+// work. mx and r are valid only after tmem_ld_wait_max. The maximum is exact (no rounding), the
+// same value as a max.f32 tree over r.
+__device__ __forceinline__ void tmem_ld32_max_issue(uint32_t taddr, uint32_t (&r)[32], float &mx) {
+    asm volatile(
+        "tcgen05.ld.red.sync.aligned.32x32b.x32.max.f32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+        "%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, %32, "
+        "[%33];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31]), "=f"(mx)
+        : "r"(taddr));
+}
 // Wait for every issued TMEM load; the register operands tie r to the wait so the compiler
 // cannot read them earlier.
 __device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
@@ -321,6 +341,31 @@ __global__ void absmax_kernel(const float *__restrict__ x, int64_t count,
     if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
 
+// Column terms of one screen launch, computed once instead of by every epilogue warp that
+// reads the columns: colp = (1 - C_B) p (+inf on padding rows), colc = core * s2 (Borůvka; 0
+// past n), and for every 32-column chunk (min colp, min colc) (0 for colc in the kNN modes).
+// One thread per padded row; n_pad is a multiple of the 256-thread block.
+__global__ void screen_columns_kernel(const float *__restrict__ pnorm,
+                                      const float *__restrict__ core, int64_t n,
+                                      float one_minus_cb, float s2, float *__restrict__ colp,
+                                      float *__restrict__ colc, float2 *__restrict__ cmin) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float p = pnorm[j] * one_minus_cb;
+    colp[j] = p;
+    float c = 0.0f;
+    if (core) {
+        c = j < n ? core[j] * s2 : 0.0f;
+        colc[j] = c;
+    }
+    float pm = p, cm = c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pm = fminf(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+        cm = fminf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+    }
+    if ((threadIdx.x & 31) == 0) cmin[j >> 5] = make_float2(pm, cm);
+}
+
 __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t *__restrict__ chunk_lo,
                                   const int32_t *__restrict__ chunk_hi, int64_t n_tiles,
                                   int64_t n_chunks, float *__restrict__ tile_mmax,
@@ -356,11 +401,6 @@ __global__ void tile_stats_kernel(const float *__restrict__ mnorm, const int32_t
 // CTAs drift apart over the waves of the persistent loop and the sweep reads the copy from
 // DRAM about a thousand times over.
 constexpr int64_t WARM = 4;
-__device__ __forceinline__ float fmax3(float a, float b, float c) {
-    float r;
-    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
-    return r;
-}
 
 // Order-preserving map of f32 values to u32 (for integer warp reductions) and back.
 __device__ __forceinline__ uint32_t f2ord(float f) {
@@ -375,18 +415,6 @@ __device__ __forceinline__ float warp_max_f(float v) {
 }
 __device__ __forceinline__ float warp_min_f(float v) {
     return ord2f(__reduce_min_sync(0xffffffffu, f2ord(v)));
-}
-
-// Largest of 32 values with three-input maxima.
-__device__ __forceinline__ float max32(const float (&v)[32]) {
-    float t[12];
-#pragma unroll
-    for (int i = 0; i < 10; ++i) t[i] = fmax3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
-    t[10] = v[30];
-    t[11] = v[31];
-    const float u0 = fmax3(t[0], t[1], t[2]), u1 = fmax3(t[3], t[4], t[5]);
-    const float u2 = fmax3(t[6], t[7], t[8]), u3 = fmax3(t[9], t[10], t[11]);
-    return fmaxf(fmax3(u0, u1, u2), u3);
 }
 
 __device__ __forceinline__ int64_t window_start(const Params &P, int64_t qb) {
@@ -481,8 +509,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     const uint32_t b_bytes = (uint32_t)P.nbk * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
-    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][PB_STRIDE]
-    float *vstage = pbuf + EPI_WARPS * PB_STRIDE;                    // [EPI_WARPS][32][VSTRIDE]
+    float *vstage = (float *)(sB + (size_t)P.stages * b_bytes);    // [EPI_WARPS][32][VSTRIDE]
     uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
     uint64_t *full = bars;
     uint64_t *empty = bars + P.stages;
@@ -491,11 +518,13 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     uint64_t *t_full = a_full + 2;   // [2]
     uint64_t *t_empty = a_full + 4;  // [2]
     uint64_t *done = a_full + 6;     // MMA drain on the abort path
-    uint64_t *rot_full = a_full + 7;    // [4] kNN sweeps: the producer published a rotation
-    uint64_t *rot_empty = a_full + 11;  // [4] every epilogue warp has read it
+    // kNN sweeps: ring of the blocks the producer took and their rotations
+    uint64_t *rot_full = a_full + 7;    // [4] the producer published a block
+    uint64_t *rot_empty = a_full + 11;  // [4] the MMA warp and every epilogue warp have read it
     uint32_t *tmem_slot = (uint32_t *)(a_full + 15);
     volatile int *abort = (volatile int *)(tmem_slot + 1);
-    int32_t *rot_val = (int32_t *)(tmem_slot + 2);  // [4]
+    int32_t *rot_val = (int32_t *)(tmem_slot + 2);  // [4] rotations
+    int64_t *rot_blk = (int64_t *)(tmem_slot + 6);  // [4] query blocks (n_qblocks: none left)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -512,7 +541,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         }
         for (int r = 0; r < 4; ++r) {
             mbar_init(&rot_full[r], 1);
-            mbar_init(&rot_empty[r], EPI_WARPS);
+            mbar_init(&rot_empty[r], EPI_WARPS + 1);
         }
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -537,8 +566,27 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             // parity of the last fill of each stage (bit 1 set = a fill was issued)
             uint32_t issued[4] = {0, 0, 0, 0};
             uint32_t a_issued = 0;
-            uint32_t li = 0;  // this CTA's query step
-            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x, ++li) {
+            for (uint32_t li = 0; !*abort; ++li) {  // li: this CTA's query step
+                int64_t qi = blockIdx.x + (int64_t)li * gridDim.x;
+                int32_t rot = 0;
+                if (ROT) {
+                    // kNN sweeps: blocks come from a global counter, so that CTAs that run faster
+                    // take more of them. The block and its rotation of the shared order (the
+                    // CTAs' average position: tiles issued so far over the grid) go to the MMA
+                    // and epilogue warps through the ring; n_qblocks there ends their loops.
+                    qi = (int64_t)atomicAdd(P.cursor + 1, 1ull);
+                    if (qi > P.n_qblocks) qi = P.n_qblocks;
+                    if (P.n_tiles > WARM && qi < P.n_qblocks) {
+                        const unsigned long long all = *(volatile unsigned long long *)P.cursor;
+                        rot = (int32_t)((all / gridDim.x) % (unsigned long long)(P.n_tiles - WARM));
+                    }
+                    const uint32_t rs = li & 3;
+                    if (!mbar_wait(&rot_empty[rs], ((li >> 2) & 1) ^ 1, abort, P.error)) break;
+                    rot_blk[rs] = qi;
+                    rot_val[rs] = rot;
+                    mbar_arrive(&rot_full[rs]);
+                }
+                if (qi >= P.n_qblocks) break;
                 const int64_t qb = block_at<SYM>(P, qi);
                 if (!mbar_wait(a_empty, a_phase ^ 1, abort, P.error)) break;
                 a_issued = 2u | a_phase;
@@ -552,19 +600,6 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
-                // kNN sweeps: the block's rotation of the shared order (the CTAs' average
-                // position: tiles issued so far over the grid), published to the epilogue warps
-                int32_t rot = 0;
-                if (ROT) {
-                    if (P.n_tiles > WARM) {
-                        const unsigned long long all = *(volatile unsigned long long *)P.cursor;
-                        rot = (int32_t)((all / gridDim.x) % (unsigned long long)(P.n_tiles - WARM));
-                    }
-                    const uint32_t rs = li & 3;
-                    if (!mbar_wait(&rot_empty[rs], ((li >> 2) & 1) ^ 1, abort, P.error)) break;
-                    rot_val[rs] = rot;
-                    mbar_arrive(&rot_full[rs]);
-                }
                 for (int64_t i = 0; i < nvis; ++i) {
                     const int64_t t = ROT ? (int64_t)knn_tile((int32_t)P.n_tiles, (int32_t)wa, rot, (int32_t)i)
                                           : vis_tile<SYM>(P, qb, wa, i);
@@ -603,7 +638,15 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             uint32_t phase = 0, a_phase = 0;
             uint32_t tcount = 0, a_commits = 0;
             const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
-            for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
+            for (uint32_t li = 0; !*abort; ++li) {
+                int64_t qi = blockIdx.x + (int64_t)li * gridDim.x;
+                if (ROT) {  // kNN sweeps: the block the producer took
+                    const uint32_t rs = li & 3;
+                    if (!mbar_wait(&rot_full[rs], (li >> 2) & 1, abort, P.error)) break;
+                    qi = *(volatile int64_t *)&rot_blk[rs];
+                    mbar_arrive(&rot_empty[rs]);
+                }
+                if (qi >= P.n_qblocks) break;
                 const int64_t qb = block_at<SYM>(P, qi);
                 if (!mbar_wait(a_full, a_phase, abort, P.error)) break;
                 a_phase ^= 1;
@@ -672,23 +715,23 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         const int quad = warp & 3;            // TMEM lane quadrant of this warp
         const int half = ew >> 2;             // column half of each tile
         const int row_local = quad * 32 + lane;
-        float *my_pb = pbuf + ew * PB_STRIDE;
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
-        const bool debug = P.debug_tile != nullptr && blockIdx.x == 0;
         uint32_t tcount = 0;
-        for (int64_t qi = blockIdx.x; qi < P.n_qblocks && !*abort; qi += gridDim.x) {
-            const int64_t qb = block_at<SYM>(P, qi);
-            // kNN sweeps: the block's rotation, published by the producer (li: this CTA's query
-            // step)
+        for (uint32_t li = 0; !*abort; ++li) {
+            int64_t qi = blockIdx.x + (int64_t)li * gridDim.x;
             int32_t rot = 0;
-            if (ROT) {
-                const uint32_t li = (uint32_t)((qi - blockIdx.x) / gridDim.x);
+            if (ROT) {  // kNN sweeps: the block the producer took and its rotation
                 const uint32_t rs = li & 3;
                 if (!mbar_wait(&rot_full[rs], (li >> 2) & 1, abort, P.error)) break;
+                qi = *(volatile int64_t *)&rot_blk[rs];
                 rot = *(volatile int32_t *)&rot_val[rs];
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&rot_empty[rs]);
             }
+            if (qi >= P.n_qblocks) break;
+            const int64_t qb = block_at<SYM>(P, qi);
+            // the debug entry point dumps query block 0 against tile 0 (its first tile)
+            const bool debug = P.debug_tile != nullptr && qb == 0;
             const int64_t row = qb * BM + row_local;  // query row
             const bool valid = row < P.nq;
             const int64_t self = valid && P.qpos ? (int64_t)P.qpos[row] : row;
@@ -745,27 +788,18 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
                 return i;
             };
-            // per-tile column data, fetched one tile ahead
-            float4 pre_p = make_float4(0, 0, 0, 0), pre_c = make_float4(0, 0, 0, 0);
-            float4 pre_m = make_float4(0, 0, 0, 0);
+            // per-tile column data, fetched one tile ahead: the chunk minima of this warp's four
+            // chunks (the per-column terms are read where a chunk is tested pair by pair)
+            float4 pre_k01 = make_float4(0, 0, 0, 0), pre_k23 = make_float4(0, 0, 0, 0);
             int32_t pre_ch = -2;
             float pre_mt = 0.0f, pre_cb = CUSCAN_INF;
             float4 pre_t = make_float4(0, 0, 0, 0);  // symmetric mode: column row bounds (raw)
             auto prefetch = [&](int64_t t) {
                 const int64_t col = t * BN + half * HALF + lane * 4;
-                pre_p = *reinterpret_cast<const float4 *>(P.pnorm + col);
-                pre_m = *reinterpret_cast<const float4 *>(P.mnorm + col);
+                pre_k01 = P.cmin[t * 4 + half * 2];
+                pre_k23 = P.cmin[t * 4 + half * 2 + 1];
                 pre_mt = P.tile_mmax[t];
                 if (BORUVKA) {
-                    // core has n entries (no padding): guard the ragged end element by element
-                    if (col + 4 <= P.n) {
-                        pre_c = *reinterpret_cast<const float4 *>(P.core + col);
-                    } else {
-                        pre_c.x = col + 0 < P.n ? P.core[col + 0] : 0.0f;
-                        pre_c.y = col + 1 < P.n ? P.core[col + 1] : 0.0f;
-                        pre_c.z = col + 2 < P.n ? P.core[col + 2] : 0.0f;
-                        pre_c.w = col + 3 < P.n ? P.core[col + 3] : 0.0f;
-                    }
                     const int64_t ch = t * 8 + half * 4 + (lane & 3);
                     pre_ch = -2;
                     if (lane < 8 && ch < P.n_chunks) pre_ch = lane < 4 ? P.chunk_lo[ch] : P.chunk_hi[ch];
@@ -787,37 +821,16 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int64_t t = t_at;
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
-                float *pb = my_pb + b * HALF;
-                float *cb = my_pb + (2 + b) * HALF;
-                float *mb = my_pb + (4 + b) * HALF;
-                const float2 *chunk_min = reinterpret_cast<const float2 *>(my_pb + 6 * HALF + b * 8);
-                {
-                    const float sc = P.one_minus_cb;
-                    const float4 pv =
-                        make_float4(pre_p.x * sc, pre_p.y * sc, pre_p.z * sc, pre_p.w * sc);
-                    reinterpret_cast<float4 *>(pb)[lane] = pv;
-                    reinterpret_cast<float4 *>(mb)[lane] = pre_m;
-                    float pmin = fminf(fminf(pv.x, pv.y), fminf(pv.z, pv.w));
-                    float cmin = 0.0f;
-                    // cores and the component bound come in raw units; the values fetched one
-                    // tile ahead are scaled only here, where they are consumed, so that the
-                    // loads stay in flight behind the previous tile's work
-                    if (BORUVKA) {
-                        const float4 cv = make_float4(pre_c.x * P.s2, pre_c.y * P.s2,
-                                                      pre_c.z * P.s2, pre_c.w * P.s2);
-                        reinterpret_cast<float4 *>(cb)[lane] = cv;
-                        cmin = fminf(fminf(cv.x, cv.y), fminf(cv.z, cv.w));
-                    }
-                    // minima over each 32-column chunk (8 lanes of 4 columns)
-#pragma unroll
-                    for (int o = 1; o < 8; o <<= 1) {
-                        pmin = fminf(pmin, __shfl_xor_sync(0xffffffffu, pmin, o));
-                        if (BORUVKA) cmin = fminf(cmin, __shfl_xor_sync(0xffffffffu, cmin, o));
-                    }
-                    if ((lane & 7) == 0)
-                        reinterpret_cast<float2 *>(my_pb + 6 * HALF + b * 8)[lane >> 3] =
-                            make_float2(pmin, cmin);
-                }
+                // this warp's columns: scaled norms pb, norms mb and (Borůvka) scaled cores cb,
+                // and (min pb, min cb) of each 32-column chunk
+                const int64_t col0 = t * BN + half * HALF;
+                const float *pb = P.colp + col0;
+                const float *mb = P.mnorm + col0;
+                const float *cb = BORUVKA ? P.colc + col0 : nullptr;
+                const float2 chunk_min[4] = {make_float2(pre_k01.x, pre_k01.y),
+                                             make_float2(pre_k01.z, pre_k01.w),
+                                             make_float2(pre_k23.x, pre_k23.y),
+                                             make_float2(pre_k23.z, pre_k23.w)};
                 // symmetric mode: the largest column row bound of each chunk (scaled)
                 float chunk_tmax[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 if (SYM) {
@@ -837,55 +850,31 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 fence_after();
                 const uint32_t taddr =
                     tmem_base + ((uint32_t)(quad * 32) << 16) + b * BN + half * HALF;
-                // Phase 1: the largest dot product of each 32-column chunk (TMEM loads are
-                // software pipelined in the threshold modes: the next chunk is in flight while
-                // one is reduced; the kNN list leaves no room for the second buffer).
+                // Phase 1: the largest dot product of each 32-column chunk, from the TMEM loads
+                // themselves (tcgen05.ld.red); two chunks per wait, as the kNN lists leave room
+                // for two 32-column loads in flight.
                 // Phase 2: one coarse test per chunk against this tile's thresholds and one warp
                 // vote per tile; the chunks that pass are read again from TMEM (the buffer is
                 // released only after this tile) and tested element by element.
-                constexpr bool PIPE = APPEND;
                 float vmax[HALF / 32];
-                if constexpr (PIPE) {
+#pragma unroll
+                for (int c = 0; c < HALF / 32; c += 2) {
                     uint32_t rA[32], rB[32];
-                    tmem_ld32_issue(taddr, rA);
+                    tmem_ld32_max_issue(taddr + c * 32, rA, vmax[c]);
+                    tmem_ld32_max_issue(taddr + (c + 1) * 32, rB, vmax[c + 1]);
                     tmem_ld_wait(rA);
-#pragma unroll
-                    for (int c = 0; c < HALF / 32; ++c) {
-                        if (c > 0) {
-#pragma unroll
-                            for (int e = 0; e < 32; ++e) rA[e] = rB[e];
-                        }
-                        if (c + 1 < HALF / 32) tmem_ld32_issue(taddr + (c + 1) * 32, rB);
-                        float v[32];
-#pragma unroll
-                        for (int e = 0; e < 32; ++e) v[e] = __uint_as_float(rA[e]);
-                        vmax[c] = max32(v);
-                        if (c + 1 < HALF / 32) tmem_ld_wait(rB);
-                    }
-                } else {
-                    // kNN lists: two chunks per wait (the lists leave no room to pipeline)
-#pragma unroll
-                    for (int c = 0; c < HALF / 32; c += 2) {
-                        uint32_t rA[32], rB[32];
-                        tmem_ld32_issue(taddr + c * 32, rA);
-                        tmem_ld32_issue(taddr + (c + 1) * 32, rB);
-                        tmem_ld_wait(rA);
-                        tmem_ld_wait(rB);
-                        float v[32], w[32];
+                    tmem_ld_wait(rB);
+                    asm volatile("" : "+f"(vmax[c]), "+f"(vmax[c + 1]));
+                    if (debug && t == 0) {
 #pragma unroll
                         for (int e = 0; e < 32; ++e) {
-                            v[e] = __uint_as_float(rA[e]);
-                            w[e] = __uint_as_float(rB[e]);
+                            P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = __uint_as_float(rA[e]);
+                            P.debug_tile[row_local * BN + half * HALF + (c + 1) * 32 + e] = __uint_as_float(rB[e]);
                         }
-                        if (debug && tcount == 0) {
-#pragma unroll
-                            for (int e = 0; e < 32; ++e) {
-                                P.debug_tile[row_local * BN + half * HALF + c * 32 + e] = v[e];
-                                P.debug_tile[row_local * BN + half * HALF + (c + 1) * 32 + e] = w[e];
-                            }
+                        if (P.debug_chunk) {
+                            P.debug_chunk[row_local * 8 + half * 4 + c] = vmax[c];
+                            P.debug_chunk[row_local * 8 + half * 4 + c + 1] = vmax[c + 1];
                         }
-                        vmax[c] = max32(v);
-                        vmax[c + 1] = max32(w);
                     }
                 }
                 // Thresholds moved to the scale of F = (1 - C_B) p_j - 2 dot with the tile's
@@ -1557,7 +1546,7 @@ static bool refined_layout(int64_t n, int d, Layout &L, bool split = false) {
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
     const size_t a = (size_t)L.nbk * KBLOCK_A, b = (size_t)L.nbk * KBLOCK_B;
-    const size_t fixed = a + (size_t)EPI_WARPS * PB_STRIDE * 4 + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+    const size_t fixed = a + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
                          256 + 1024;
     int st = (int)((227 * 1024 - fixed) / b);
     if (st > 4) st = 4;
@@ -1580,6 +1569,7 @@ size_t refined_workspace_bytes(int64_t n, int d, int k) {
     const size_t copy_cols = (size_t)L.d_pad * (L.d_pad <= 64 ? 2 : 1);
     size_t b = (size_t)L.n_pad * copy_cols * 2 + 2 * sizeof(float) * (size_t)L.n_pad;  // xt, norms
     b += 3 * sizeof(float) * (size_t)L.n_tiles + 64;          // tile stats, flags, cursor
+    b += 2 * sizeof(float) * (size_t)L.n_pad + sizeof(float) * (size_t)L.n_pad / 16;  // column terms
     b += sizeof(int32_t) * (size_t)n;                                                 // fallback
     b += 2 * 4 * (size_t)n * 2 * M;                  // candidate ids and bounds (two lists of M)
     b += sizeof(uint32_t) * (size_t)n + 2 * sizeof(int32_t) * (size_t)n;  // cbound, rowcnt
@@ -1711,6 +1701,7 @@ template <int M, int MODE>
 static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64_t n, int d,
                       const float *core, const int32_t *label, const int32_t *chunk_lo,
                       const int32_t *chunk_hi, cudaStream_t s, float *debug_tile = nullptr,
+                      float *debug_chunk = nullptr,
                       const QuerySet &Q = QuerySet()) {
     constexpr bool BORUVKA = MODE == MODE_BORUVKA || MODE == MODE_BORUVKA_SYM;
     int rc = ensure(ctx, R.cand_ids, sizeof(int32_t) * n * 2 * M, "screen candidates");
@@ -1755,6 +1746,7 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.cand_lb = as<float>(R.cand_lb);
     P.error = as<int>(R.error);
     P.debug_tile = debug_tile;
+    P.debug_chunk = debug_chunk;
     P.c_b = cb;
     P.cap = BORUVKA_CAP;
     if (BORUVKA) {
@@ -1780,6 +1772,18 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     if (P.n_qblocks == 0) return CUSCAN_OK;
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.error.ptr, 0, 16, s));
     CUSCAN_CUDA(ctx, cudaMemsetAsync(R.cursor.ptr, 0, 16, s));
+    // the column terms of this launch (its C_B and, for Borůvka, the core scale)
+    if (int rc = ensure(ctx, R.colp, sizeof(float) * L.n_pad, "screen column norms")) return rc;
+    if (BORUVKA)
+        if (int rc = ensure(ctx, R.colc, sizeof(float) * L.n_pad, "screen column cores")) return rc;
+    if (int rc = ensure(ctx, R.cmin, sizeof(float) * L.n_pad / 16, "screen chunk minima")) return rc;
+    P.colp = as<float>(R.colp);
+    P.colc = BORUVKA ? as<float>(R.colc) : nullptr;
+    P.cmin = as<float4>(R.cmin);
+    CUSCAN_KERNEL(screen_columns_kernel, (unsigned)(L.n_pad / 256), 256, 0, s, P.pnorm,
+                  BORUVKA ? core : nullptr, n, P.one_minus_cb, P.s2, as<float>(R.colp),
+                  BORUVKA ? as<float>(R.colc) : nullptr, as<float2>(R.cmin));
+    CUSCAN_LAUNCH(ctx, "screen_columns_kernel");
     auto kernel = screen_kernel<M, MODE>;
     if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
     int64_t grid = P.n_qblocks < ctx->sm_count ? P.n_qblocks : ctx->sm_count;
@@ -1916,7 +1920,7 @@ int launch_knn_refined(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_
         Q.cand_ids = as<int32_t>(R.cand2);
         Q.rowcnt = as<int32_t>(R.rowcnt2);
         if ((rc = run_screen<M, MODE_KNN_THRESHOLD>(ctx, R, L, n, d, nullptr, nullptr, nullptr,
-                                                   nullptr, s, nullptr, Q)))
+                                                   nullptr, s, nullptr, nullptr, Q)))
             return rc;
         CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, sizeof(int), s));
         if ((rc = allow_dynamic_smem(ctx, rerank_knn_threshold_kernel, rr_smem))) return rc;
@@ -2037,13 +2041,13 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
         Q.nq = nq;
         Q.qpos = qpos;
         Q.rowlb = as<float>(R.lbtmp);
-        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, Q);
+        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, nullptr, Q);
     } else if (sym) {
         rc = run_screen<M, MODE_BORUVKA_SYM>(ctx, R, L, n, d, corep, labp, clo, chi, s);
     } else {
         QuerySet Q;
         Q.rowlb = as<float>(R.lbtmp);
-        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, Q);
+        rc = run_screen<M, MODE_BORUVKA>(ctx, R, L, n, d, corep, labp, clo, chi, s, nullptr, nullptr, Q);
     }
     if (rc) return rc;
     if (!sym && nq > 0) {
@@ -2089,8 +2093,8 @@ __global__ void debug_rows_kernel(const float *__restrict__ pnorm, const float *
 }
 
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
-                      int operands, float *out, float *rows_out, float *scale_out,
-                      cudaStream_t s) {
+                      int operands, float *out, float *rows_out, float *chunk_out,
+                      float *scale_out, cudaStream_t s) {
     RefinedBuffers &R = b.refined;
     R.have_scale = false;
     R.want_fp16 = operands == FMT_FP16;
@@ -2105,7 +2109,9 @@ int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t
                     R.split ? " (split copies need d <= 64)" : "");
     if (scale_out) *scale_out = R.fp16 ? R.scale : 1.0f;
     rc = prep(ctx, R, L, x, n, d, nullptr, nullptr, s);
-    if (!rc) rc = run_screen<32, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s, out);
+    if (!rc)
+        rc = run_screen<32, MODE_KNN_LIST>(ctx, R, L, n, d, nullptr, nullptr, nullptr, nullptr, s,
+                                           out, chunk_out);
     if (!rc && rows_out) {
         float ca, cb, abs_c;
         error_coefficients(d, L.d_pad, operand_format(R), R.fp16 ? R.amax_value * R.scale : R.amax_value, ca, cb, abs_c);

@@ -302,11 +302,13 @@ int cuscan_debug_screen_tile(cuscan_ctx *ctx, const float *data, int64_t n, int3
  * bf16 (hi.hi' + hi.lo' + lo.hi', d <= 64). With rows_out (device, float[n][4]) every row's
  * bound terms (ps, pb, cm, m) are written, ps = (1 - C_B) p - abs_c, pb = (1 - C_B) p,
  * cm = C_A m, so that the screen's lower bound of entry (r, c) is
- * fmaf(-cm_r, m_c, fmaf(-2, tile[r][c], pb_c) + ps_r), in screen units.
+ * fmaf(-cm_r, m_c, fmaf(-2, tile[r][c], pb_c) + ps_r), in screen units. With chunk_out (device,
+ * float[128][8]) the screen's phase-1 maxima of the tile's 32-column chunks are written: entry
+ * (r, h) is the largest of tile[r][32 h .. 32 h + 31], as the TMEM load returned it.
  */
 int cuscan_debug_screen_tile_operands(cuscan_ctx *ctx, const float *data, int64_t n, int32_t d,
                                       int32_t operands, float *tile_out, float *rows_out,
-                                      float *scale_out, void *stream);
+                                      float *chunk_out, float *scale_out, void *stream);
 
 /* ---- host-side extraction (no device work) ---- */
 

@@ -195,6 +195,44 @@ def test_tensor_core_tile_matches_bf16_products(gpu_ctx, n, d, seed):
     assert np.all(err <= 1e-5 * scale + 1e-30), float(np.max(err / np.maximum(scale, 1e-30)))
 
 
+def _chunk_max_data(kind: str, n: int, d: int) -> np.ndarray:
+    rng = np.random.default_rng(d + len(kind))
+    if kind == "normal":
+        return rng.normal(size=(n, d)).astype(np.float32)
+    if kind == "negative_dots":  # queries and references on opposite sides: all dots < 0
+        x = np.abs(rng.normal(size=(n, d))) + 0.1
+        x[:128] *= -1.0
+        return x.astype(np.float32)
+    if kind == "ties":  # few distinct values: many equal dots, signed zeros
+        return rng.integers(-1, 2, size=(n, d)).astype(np.float32)
+    if kind == "wide_range":
+        return (rng.normal(size=(n, d)) * np.exp2(rng.integers(-20, 20, size=(n, 1)))).astype(
+            np.float32)
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("d", [64, 128])
+@pytest.mark.parametrize("kind", ["normal", "negative_dots", "ties", "wide_range"])
+def test_chunk_maxima_equal_the_tile_maxima(gpu_ctx, kind, d):
+    """The screens take each row's largest dot product per 32-column chunk from the TMEM load
+    itself (tcgen05.ld.red .max): it must equal the maximum of the 32 loaded accumulator values
+    bit for bit, for every row of the 128-row block and every chunk of the 256-column tile
+    (lane r holds row r, chunk h covers columns 32 h .. 32 h + 31)."""
+    n = 512
+    x = _chunk_max_data(kind, n, d)
+    tx = dev(x)
+    out = torch.zeros((128, 256), dtype=torch.float32, device="cuda")
+    chunks = torch.full((128, 8), float("nan"), dtype=torch.float32, device="cuda")
+    gpu_ctx.debug_screen_tile(ptr(tx), n, d, ptr(out), stream(), chunk_out=ptr(chunks))
+    torch.cuda.synchronize()
+    tile = out.cpu().numpy()
+    got = chunks.cpu().numpy()
+    expect = tile.reshape(128, 8, 32).max(axis=2)
+    assert not np.isnan(got).any()
+    np.testing.assert_array_equal(bits(np.abs(got)), bits(np.abs(expect)))
+    np.testing.assert_array_equal(got, expect)
+
+
 def test_component_reduce_clamps_a_malformed_plan(gpu_ctx):
     """Plan arrays that overrun their buffers (partial offsets past p, tile ends past n, member
     ids >= n) are clamped instead of read out of bounds: the result equals the same call on
