@@ -46,6 +46,7 @@ constexpr uint32_t KBLOCK_B = BN * 128;   // bytes of one 64-element K block of 
 constexpr uint64_t WAIT_NS = 2000000000ull;  // bounded mbarrier waits: 2 s of wall time
 constexpr uint32_t WAIT_POLLS = 1u << 22;      // poll bound of the abort-path drains
 constexpr int VSTRIDE = 36;               // floats per lane in the hit staging area
+constexpr int PB_STRIDE = 4 * HALF;       // kNN modes, per epilogue warp: [2][HALF] pb, [2][HALF] m
 constexpr int BORUVKA_CAP = 32;           // Borůvka candidate slots per row half
 
 struct Params {
@@ -503,13 +504,17 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
     constexpr bool THRESH = MODE == MODE_KNN_THRESHOLD;
     constexpr bool APPEND = BORUVKA || THRESH;  // threshold modes append to per-row buffers
     constexpr bool ROT = !BORUVKA;              // kNN sweeps: rotated shared tile order
+    // kNN sweeps: the column terms of each tile are copied into the warp's shared slots, where
+    // the list insertions read them (Borůvka screens read them from global memory)
+    constexpr bool STAGE = !BORUVKA;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t a_bytes = (uint32_t)P.nbk * KBLOCK_A;
     const uint32_t b_bytes = (uint32_t)P.nbk * KBLOCK_B;
     uint8_t *sA = smem;
     uint8_t *sB = smem + a_bytes;
-    float *vstage = (float *)(sB + (size_t)P.stages * b_bytes);    // [EPI_WARPS][32][VSTRIDE]
+    float *pbuf = (float *)(sB + (size_t)P.stages * b_bytes);      // [EPI_WARPS][PB_STRIDE]
+    float *vstage = pbuf + EPI_WARPS * PB_STRIDE;                    // [EPI_WARPS][32][VSTRIDE]
     uint64_t *bars = (uint64_t *)(vstage + EPI_WARPS * 32 * VSTRIDE);
     uint64_t *full = bars;
     uint64_t *empty = bars + P.stages;
@@ -716,6 +721,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
         const int half = ew >> 2;             // column half of each tile
         const int row_local = quad * 32 + lane;
         float *my_v = vstage + (ew * 32 + lane) * VSTRIDE;
+        float *my_pb = pbuf + ew * PB_STRIDE;
         uint32_t tcount = 0;
         for (uint32_t li = 0; !*abort; ++li) {
             int64_t qi = blockIdx.x + (int64_t)li * gridDim.x;
@@ -794,11 +800,21 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             int32_t pre_ch = -2;
             float pre_mt = 0.0f, pre_cb = CUSCAN_INF;
             float4 pre_t = make_float4(0, 0, 0, 0);  // symmetric mode: column row bounds (raw)
-            auto prefetch = [&](int64_t t) {
+            auto prefetch = [&](int64_t t, uint32_t slot) {
                 const int64_t col = t * BN + half * HALF + lane * 4;
                 pre_k01 = P.cmin[t * 4 + half * 2];
                 pre_k23 = P.cmin[t * 4 + half * 2 + 1];
                 pre_mt = P.tile_mmax[t];
+                if (STAGE) {  // straight into the tile's shared slots (no registers)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                     smem_u32(my_pb + slot * HALF + lane * 4)),
+                                 "l"(P.colp + col)
+                                 : "memory");
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                                     smem_u32(my_pb + (2 + slot) * HALF + lane * 4)),
+                                 "l"(P.mnorm + col)
+                                 : "memory");
+                }
                 if (BORUVKA) {
                     const int64_t ch = t * 8 + half * 4 + (lane & 3);
                     pre_ch = -2;
@@ -815,7 +831,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
             };
             int64_t ti = next_index(0);
-            if (ti < nvis) prefetch(t_at);
+            if (ti < nvis) prefetch(t_at, tcount & 1);
             bool ok = true;
             while (ti < nvis) {
                 const int64_t t = t_at;
@@ -824,9 +840,13 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 // this warp's columns: scaled norms pb, norms mb and (Borůvka) scaled cores cb,
                 // and (min pb, min cb) of each 32-column chunk
                 const int64_t col0 = t * BN + half * HALF;
-                const float *pb = P.colp + col0;
-                const float *mb = P.mnorm + col0;
+                const float *pb = STAGE ? my_pb + b * HALF : P.colp + col0;
+                const float *mb = STAGE ? my_pb + (2 + b) * HALF : P.mnorm + col0;
                 const float *cb = BORUVKA ? P.colc + col0 : nullptr;
+                if (STAGE) {  // this tile's column terms, copied one tile ahead
+                    asm volatile("cp.async.wait_all;" ::: "memory");
+                    __syncwarp();
+                }
                 const float2 chunk_min[4] = {make_float2(pre_k01.x, pre_k01.y),
                                              make_float2(pre_k01.z, pre_k01.w),
                                              make_float2(pre_k23.x, pre_k23.y),
@@ -845,7 +865,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
-                if (ti_next < nvis) prefetch(t_at);
+                if (ti_next < nvis) prefetch(t_at, b ^ 1);
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -1133,6 +1153,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 }
             }
         }
+        // copies of column terms still in flight (a loop left early) land before the CTA exits
+        if (STAGE) asm volatile("cp.async.wait_all;" ::: "memory");
     }
     fence_before();
     __syncthreads();
@@ -1546,7 +1568,7 @@ static bool refined_layout(int64_t n, int d, Layout &L, bool split = false) {
     L.n_pad = L.n_tiles * BN;
     L.n_qblocks = ceil_div(n, BM);
     const size_t a = (size_t)L.nbk * KBLOCK_A, b = (size_t)L.nbk * KBLOCK_B;
-    const size_t fixed = a + (size_t)EPI_WARPS * 32 * VSTRIDE * 4 +
+    const size_t fixed = a + (size_t)EPI_WARPS * (PB_STRIDE + 32 * VSTRIDE) * 4 +
                          256 + 1024;
     int st = (int)((227 * 1024 - fixed) / b);
     if (st > 4) st = 4;
