@@ -276,13 +276,12 @@ def serving_run(args, precision: str) -> dict:
     import torch
 
     from cuscan_gb300 import synthetic
-    from cuscan_gb300.serving import FitServer
+    from cuscan_gb300.serving import FitServer, default_budget
 
     specs = synthetic.fit_request_stream(args.serve_requests)
     pool_n = min(args.serve_pool, len(specs))
     pool = [synthetic.request_points(specs[i]) for i in range(pool_n)]
-    free, _ = torch.cuda.mem_get_info()
-    budget = int(0.5 * free)
+    budget = default_budget()  # 9/10 of free device memory less 64 MiB
 
     def kwargs(i):
         sp = specs[i % pool_n]
@@ -400,13 +399,12 @@ def small_fit_packing_section(args) -> dict:
     import torch
 
     from cuscan_gb300 import _lib, synthetic
-    from cuscan_gb300.serving import FitServer
+    from cuscan_gb300.serving import FitServer, default_budget
 
     specs = [sp for sp in synthetic.fit_request_stream(args.serve_requests)
              if sp["n"] <= _lib.PACK_MAX_ROWS][:1000]
     points = [synthetic.request_points(sp) for sp in specs]
-    free, _ = torch.cuda.mem_get_info()
-    budget = int(0.5 * free)
+    budget = default_budget()  # 9/10 of free device memory less 64 MiB
     out = {"requests": len(specs), "slots": args.serve_slots, "precision": "fp16_refined"}
     for limit in (1, 8):
         with FitServer(slots=args.serve_slots, budget_bytes=budget, pack_limit=limit) as srv:
@@ -438,7 +436,7 @@ def mixed_serving_section(args) -> dict:
 
     import cuscan_gb300 as cg
     from cuscan_gb300 import synthetic
-    from cuscan_gb300.serving import FitServer
+    from cuscan_gb300.serving import FitServer, default_budget
 
     t_setup = time.perf_counter()
     npred = args.mixed_predictors
@@ -459,8 +457,7 @@ def mixed_serving_section(args) -> dict:
     specs = synthetic.fit_request_stream(min(256, args.serve_requests))
     fpool = [synthetic.request_points(sp) for sp in specs]
     setup_s = time.perf_counter() - t_setup
-    free, _ = torch.cuda.mem_get_info()
-    budget = int(0.5 * free)
+    budget = default_budget()  # 9/10 of free device memory less 64 MiB
     out = {"predictors": npred, "predictor_training": "n=100000, d=64, 40 blobs, fp16_refined",
            "predict_batch": "log-uniform [1, 4096] rows", "setup_s": setup_s}
 

@@ -21,6 +21,34 @@ import numpy as np
 from . import _lib
 
 
+MEMORY_RESERVE_BYTES = 64 << 20
+
+
+def usable_bytes(free_bytes: int, total_bytes: int, live_bytes: int = 0,
+                 limit_bytes: int | None = None) -> int:
+    """Device memory a plan may commit, by the reference's admission rule
+    (crates/cuscan-common/src/memory.rs:17-40): nine tenths of the free bytes (rounded down,
+    computed as (free // 10) * 9 + (free % 10) * 9 // 10), plus the bytes the caller already
+    holds, capped by an optional limit and by the total, less a 64 MiB reserve; never below 0."""
+    for v in (free_bytes, total_bytes, live_bytes):
+        if v < 0:
+            raise ValueError("memory sizes must be non-negative")
+    free = (free_bytes // 10) * 9 + (free_bytes % 10) * 9 // 10
+    usable = min(free + live_bytes, total_bytes)
+    if limit_bytes is not None:
+        usable = min(usable, limit_bytes)
+    return max(usable - MEMORY_RESERVE_BYTES, 0)
+
+
+def default_budget(device: int = 0, limit_bytes: int | None = None) -> int:
+    """The server's memory budget on `device` by the reference's rule (usable_bytes) applied
+    to the device's free and total memory now."""
+    import torch
+
+    free, total = torch.cuda.mem_get_info(device)
+    return usable_bytes(int(free), int(total), 0, limit_bytes)
+
+
 def _precision_code(precision: str) -> int:
     if precision not in _lib.PRECISIONS:
         raise ValueError("precision must be 'fp32', 'bf16_refined' or 'fp16_refined'")
@@ -28,7 +56,9 @@ def _precision_code(precision: str) -> int:
 
 
 class FitServer:
-    """Fit-request server. ``budget_bytes`` bounds the device workspace of all slots together.
+    """Fit-request server. ``budget_bytes`` bounds the device workspace of all slots together;
+    by default it is ``default_budget(device)``, the reference's admission rule on the device's
+    free memory (16 GiB for the simulated server).
 
     ``pack_limit`` is the most small fits (at most ``_lib.PACK_MAX_ROWS`` rows) a slot runs
     together in one CUDA graph launch; 1 (the default) runs every fit on its own, which is
@@ -37,8 +67,11 @@ class FitServer:
     ``simulated_us_per_kpoint`` builds the scheduling test double instead: the same queue and
     admission with slots that run no fit (no GPU needed; results cannot be read)."""
 
-    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int = 16 << 30, *,
+    def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int | None = None, *,
                  pack_limit: int = 1, simulated_us_per_kpoint: float | None = None):
+        if budget_bytes is None:
+            budget_bytes = (16 << 30 if simulated_us_per_kpoint is not None
+                            else default_budget(device))
         self._lib = _lib.load()
         handle = C.c_void_p()
         err = C.create_string_buffer(256)

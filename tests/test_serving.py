@@ -22,6 +22,28 @@ def drain(server, ids, timeout=30.0):
     return infos
 
 
+def test_usable_bytes_follows_the_reference_admission_rule():
+    """usable = min(9/10 free (exact integer form) + live, limit, total) - 64 MiB, saturating
+    at 0 (crates/cuscan-common/src/memory.rs:17-40)."""
+    from cuscan_gb300.serving import MEMORY_RESERVE_BYTES, usable_bytes
+
+    mib, gib = 1 << 20, 1 << 30
+    assert MEMORY_RESERVE_BYTES == 64 * mib
+    # 9/10 of 100 GiB less the reserve
+    assert usable_bytes(100 * gib, 200 * gib) == 90 * gib - 64 * mib
+    # rounding of the tenth: (19 // 10) * 9 + (19 % 10) * 9 // 10 = 9 + 8
+    assert usable_bytes(19 + 64 * mib * 10, 1 << 62) == (64 * mib * 9 + 17) - 64 * mib
+    # bytes already held count on top of the free share; the total and the limit cap the sum
+    assert usable_bytes(10 * gib, 100 * gib, live_bytes=5 * gib) == 14 * gib - 64 * mib
+    assert usable_bytes(10 * gib, 8 * gib, live_bytes=5 * gib) == 8 * gib - 64 * mib
+    assert usable_bytes(10 * gib, 100 * gib, limit_bytes=2 * gib) == 2 * gib - 64 * mib
+    # below the reserve nothing is usable
+    assert usable_bytes(0, 100 * gib) == 0
+    assert usable_bytes(70 * mib, 100 * gib) == 0
+    with pytest.raises(ValueError):
+        usable_bytes(-1, 100 * gib)
+
+
 def test_workspace_bound_grows_with_shape():
     small, big = bound(1000, 16), bound(50000, 128)
     assert 0 < small < big
