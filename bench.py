@@ -157,8 +157,8 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each screen kernel, from a one-pass ncu capture of
 # the full-size workload (dram__bytes_read.sum + dram__bytes_write.sum): the kNN sweep (one
 # launch per fit) and the mean over the Borůvka screen launches of one fit.
-NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_screen": 123511651584.0,
-                                              "boruvka_candidates": 773395264.0}}
+NCU_TRAFFIC = {"vmf_500k_d128:bf16_refined": {"knn_screen": 4888804352.0,
+                                              "boruvka_candidates": 1182957504.0}}
 NCU_TRAFFIC_SCOPE = {"knn_screen": "ncu dram read+write bytes of the kNN screen launch",
                      "boruvka_candidates": "ncu dram read+write bytes, mean per Borůvka screen "
                                            "launch"}

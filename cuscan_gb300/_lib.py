@@ -50,6 +50,7 @@ SIGNATURES = {
     "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                          _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
     "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
+    "cuscan_fit_core_packed_graph_stats": (C.c_int, [_VP, _I64P, _I64P]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_debug_screen_tile_operands": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32,
                                                     _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
@@ -484,6 +485,14 @@ class Context:
             o["stats"] = item.stats.as_dict()
             o["status"] = int(item.status)
         return outs
+
+    def packed_graph_stats(self) -> dict:
+        """Packs of this context whose graph was instantiated, and packs that updated the graph
+        of an earlier pack of the same size in place."""
+        inst, upd = C.c_int64(0), C.c_int64(0)
+        self.check(self._lib.cuscan_fit_core_packed_graph_stats(self.handle, C.byref(inst),
+                                                                C.byref(upd)))
+        return {"instantiations": int(inst.value), "updates": int(upd.value)}
 
 
 def clusters_from_spanning_tree(src, dst, weight, *, min_cluster_size: int,

@@ -73,32 +73,33 @@ __global__ void iota_kernel(int32_t *p, int64_t n) {
     if (i < n) p[i] = (int32_t)i;
 }
 
-__global__ void dbl_init_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ label,
-                                int64_t n, int32_t *__restrict__ jmp, int32_t *__restrict__ mx) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !active_node(label, s)) return;
+// Per-node steps of the cycle breaking and union (resolve_proposals). Each is run by one
+// thread per node, either as a kernel of its own or inside the single-CTA resolve_small_kernel;
+// the step order and the barriers between them are the same in both.
+__device__ __forceinline__ void dbl_init_at(int64_t s, const int32_t *__restrict__ next,
+                                            const int32_t *__restrict__ label,
+                                            int32_t *__restrict__ jmp, int32_t *__restrict__ mx) {
+    if (!active_node(label, s)) return;
     jmp[s] = next[s];
     mx[s] = (int32_t)s;
 }
-
-__global__ void dbl_step_kernel(const int32_t *__restrict__ jin, const int32_t *__restrict__ min_,
-                                const int32_t *__restrict__ label, int64_t n,
-                                int32_t *__restrict__ jout, int32_t *__restrict__ mout) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !active_node(label, s)) return;
+__device__ __forceinline__ void dbl_step_at(int64_t s, const int32_t *__restrict__ jin,
+                                            const int32_t *__restrict__ min_,
+                                            const int32_t *__restrict__ label,
+                                            int32_t *__restrict__ jout, int32_t *__restrict__ mout) {
+    if (!active_node(label, s)) return;
     int32_t j = jin[s];
     jout[s] = jin[j];
     int32_t a = min_[s], b = min_[j];
     mout[s] = a > b ? a : b;
 }
-
 // keep[s] = s proposes an edge that is not its cycle's largest-label edge; parent[s] is the
 // forest parent after the skipped edges are removed.
-__global__ void keep_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ jmp,
-                            const int32_t *__restrict__ mx, const int32_t *__restrict__ label,
-                            int64_t n, int32_t *__restrict__ keep, int32_t *__restrict__ parent) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+__device__ __forceinline__ void keep_at(int64_t s, const int32_t *__restrict__ next,
+                                        const int32_t *__restrict__ jmp,
+                                        const int32_t *__restrict__ mx,
+                                        const int32_t *__restrict__ label,
+                                        int32_t *__restrict__ keep, int32_t *__restrict__ parent) {
     if (!active_node(label, s)) {
         keep[s] = 0;
         return;
@@ -108,6 +109,67 @@ __global__ void keep_kernel(const int32_t *__restrict__ next, const int32_t *__r
     keep[s] = k ? 1 : 0;
     parent[s] = k ? t : (int32_t)s;
 }
+__device__ __forceinline__ void emit_at(int64_t s, const int32_t *__restrict__ keep,
+                                        const int32_t *__restrict__ pos,
+                                        const uint32_t *__restrict__ esrc,
+                                        const uint32_t *__restrict__ edst,
+                                        const float *__restrict__ ew, int64_t edges,
+                                        uint32_t *__restrict__ out_src,
+                                        uint32_t *__restrict__ out_dst, float *__restrict__ out_w,
+                                        int64_t capacity) {
+    if (!keep[s]) return;
+    int64_t at = edges + pos[s];
+    if (at >= capacity) return;
+    out_src[at] = esrc[s];
+    out_dst[at] = edst[s];
+    out_w[at] = ew[s];
+}
+// Path halving toward the root (in place).
+__device__ __forceinline__ void jump_at(int64_t s, int32_t *__restrict__ parent,
+                                        const int32_t *__restrict__ label) {
+    if (!active_node(label, s)) return;
+    int32_t p = parent[s];
+    int32_t pp = parent[p];
+    if (pp != p) parent[s] = pp;
+}
+__device__ __forceinline__ void minlab_init_at(int64_t s, const int32_t *__restrict__ parent,
+                                               const int32_t *__restrict__ label,
+                                               int32_t *__restrict__ minlab) {
+    if (!active_node(label, s)) return;
+    if (parent[s] == (int32_t)s) minlab[s] = (int32_t)s;
+}
+__device__ __forceinline__ void minlab_reduce_at(int64_t s, const int32_t *__restrict__ parent,
+                                                 const int32_t *__restrict__ label,
+                                                 int32_t *__restrict__ minlab) {
+    if (!active_node(label, s)) return;
+    atomicMin(&minlab[parent[s]], (int32_t)s);
+}
+// label[i] <- smallest label of the tree that holds i's old component.
+__device__ __forceinline__ void relabel_at(int64_t i, int32_t *__restrict__ label,
+                                           const int32_t *__restrict__ parent,
+                                           const int32_t *__restrict__ minlab) {
+    label[i] = minlab[parent[label[i]]];
+}
+
+__global__ void dbl_init_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ label,
+                                int64_t n, int32_t *__restrict__ jmp, int32_t *__restrict__ mx) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dbl_init_at(s, next, label, jmp, mx);
+}
+
+__global__ void dbl_step_kernel(const int32_t *__restrict__ jin, const int32_t *__restrict__ min_,
+                                const int32_t *__restrict__ label, int64_t n,
+                                int32_t *__restrict__ jout, int32_t *__restrict__ mout) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dbl_step_at(s, jin, min_, label, jout, mout);
+}
+
+__global__ void keep_kernel(const int32_t *__restrict__ next, const int32_t *__restrict__ jmp,
+                            const int32_t *__restrict__ mx, const int32_t *__restrict__ label,
+                            int64_t n, int32_t *__restrict__ keep, int32_t *__restrict__ parent) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) keep_at(s, next, jmp, mx, label, keep, parent);
+}
 
 __global__ void emit_kernel(const int32_t *__restrict__ keep, const int32_t *__restrict__ pos,
                             const uint32_t *__restrict__ esrc, const uint32_t *__restrict__ edst,
@@ -115,12 +177,9 @@ __global__ void emit_kernel(const int32_t *__restrict__ keep, const int32_t *__r
                             uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
                             float *__restrict__ out_w, int64_t capacity) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !keep[s]) return;
-    int64_t at = (int64_t)status->edges + pos[s];
-    if (at >= capacity) return;
-    out_src[at] = esrc[s];
-    out_dst[at] = edst[s];
-    out_w[at] = ew[s];
+    if (s < n)
+        emit_at(s, keep, pos, esrc, edst, ew, (int64_t)status->edges, out_src, out_dst, out_w,
+                capacity);
 }
 
 __global__ void add_edges_kernel(DevStatus *status, const int32_t *kept_total,
@@ -134,34 +193,27 @@ __global__ void add_edges_kernel(DevStatus *status, const int32_t *kept_total,
 __global__ void jump_kernel(int32_t *__restrict__ parent, const int32_t *__restrict__ label,
                             int64_t n) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !active_node(label, s)) return;
-    int32_t p = parent[s];
-    int32_t pp = parent[p];
-    if (pp != p) parent[s] = pp;
+    if (s < n) jump_at(s, parent, label);
 }
 
 __global__ void minlab_init_kernel(const int32_t *__restrict__ parent,
                                    const int32_t *__restrict__ label, int64_t n,
                                    int32_t *__restrict__ minlab) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !active_node(label, s)) return;
-    if (parent[s] == (int32_t)s) minlab[s] = (int32_t)s;
+    if (s < n) minlab_init_at(s, parent, label, minlab);
 }
 
 __global__ void minlab_reduce_kernel(const int32_t *__restrict__ parent,
                                      const int32_t *__restrict__ label, int64_t n,
                                      int32_t *__restrict__ minlab) {
     int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || !active_node(label, s)) return;
-    atomicMin(&minlab[parent[s]], (int32_t)s);
+    if (s < n) minlab_reduce_at(s, parent, label, minlab);
 }
 
-// label[i] <- smallest label of the tree that holds i's old component.
 __global__ void relabel_kernel(int32_t *__restrict__ label, const int32_t *__restrict__ parent,
                                const int32_t *__restrict__ minlab, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    label[i] = minlab[parent[label[i]]];
+    if (i < n) relabel_at(i, label, parent, minlab);
 }
 
 __global__ void count_components_kernel(const int32_t *__restrict__ label, int64_t n,
@@ -364,6 +416,88 @@ __global__ void scan_add_kernel(int32_t *__restrict__ out, int64_t n,
     if (i < n) out[i] += sums[i / SCAN_TILE];
 }
 
+// resolve_proposals of up to SMALL_RESOLVE_ROWS nodes in one CTA: the same per-node steps in
+// the same order as the kernel sequence below, with block barriers where the sequence has
+// kernel boundaries (global writes of the block are visible to the whole block after
+// __syncthreads). One launch instead of about 33 per seed or round of a small fit. In a round
+// active_label and point_label are the same array (no __restrict__ on either).
+constexpr int64_t SMALL_RESOLVE_ROWS = 2048;
+constexpr int SMALL_ITEMS = (int)(SMALL_RESOLVE_ROWS / SCAN_THREADS);
+__global__ void __launch_bounds__(SCAN_THREADS)
+    resolve_small_kernel(const int32_t *__restrict__ next, const int32_t *active_label,
+                         int32_t *point_label, int64_t n, int steps, int32_t *ja,
+                         int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
+                         int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
+                         const uint32_t *__restrict__ esrc, const uint32_t *__restrict__ edst,
+                         const float *__restrict__ ew, int32_t *parent,
+                         int32_t *__restrict__ minlab, DevStatus *status,
+                         uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
+                         float *__restrict__ out_w, int64_t capacity, int require_progress) {
+    __shared__ int warp_sums[SCAN_THREADS / 32];
+    const int tid = threadIdx.x;
+    // cycle breaking: pointer doubling with a running maximum, ping-pong buffers
+    for (int64_t s = tid; s < n; s += SCAN_THREADS) dbl_init_at(s, next, active_label, ja, ma);
+    __syncthreads();
+    for (int t = 0; t < steps; ++t) {
+        for (int64_t s = tid; s < n; s += SCAN_THREADS)
+            dbl_step_at(s, ja, ma, active_label, jb, mb);
+        __syncthreads();
+        int32_t *tj = ja, *tm = ma;
+        ja = jb;
+        ma = mb;
+        jb = tj;
+        mb = tm;
+    }
+    for (int64_t s = tid; s < n; s += SCAN_THREADS) keep_at(s, next, ja, ma, active_label, keep, parent);
+    __syncthreads();
+    // exclusive scan of keep in node order: thread t holds nodes [t SMALL_ITEMS, +SMALL_ITEMS)
+    int v[SMALL_ITEMS];
+    int sum = 0;
+    const int64_t base = (int64_t)tid * SMALL_ITEMS;
+#pragma unroll
+    for (int u = 0; u < SMALL_ITEMS; ++u) {
+        v[u] = base + u < n ? keep[base + u] : 0;
+        sum += v[u];
+    }
+    int total;
+    int prefix = block_exclusive_scan(sum, warp_sums, total);
+#pragma unroll
+    for (int u = 0; u < SMALL_ITEMS; ++u) {
+        if (base + u < n) pos[base + u] = prefix;
+        prefix += v[u];
+    }
+    __syncthreads();
+    // append the kept edges in node order after the edges emitted so far
+    const int64_t edges = (int64_t)status->edges;
+    for (int64_t s = tid; s < n; s += SCAN_THREADS)
+        emit_at(s, keep, pos, esrc, edst, ew, edges, out_src, out_dst, out_w, capacity);
+    __syncthreads();
+    if (tid == 0) {
+        *kept_total = total;
+        status->edges += (unsigned long long)total;
+        // "Boruvka round made no progress" (mst.rs:279-283)
+        if (require_progress && total == 0) atomicCAS(&status->err_kind, 0, 4);
+    }
+    // union: path halving, smallest point of every tree, relabel, count the components
+    for (int t = 0; t < steps; ++t) {
+        for (int64_t s = tid; s < n; s += SCAN_THREADS) jump_at(s, parent, active_label);
+        __syncthreads();
+    }
+    for (int64_t s = tid; s < n; s += SCAN_THREADS) minlab_init_at(s, parent, active_label, minlab);
+    __syncthreads();
+    for (int64_t s = tid; s < n; s += SCAN_THREADS)
+        minlab_reduce_at(s, parent, active_label, minlab);
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) relabel_at(i, point_label, parent, minlab);
+    __syncthreads();
+    int roots = 0;
+    for (int64_t i0 = 0; i0 < n; i0 += SCAN_THREADS) {
+        const int64_t i = i0 + tid;
+        roots += __syncthreads_count(i < n && point_label[i] == (int32_t)i);
+    }
+    if (tid == 0) status->components = (unsigned long long)roots;
+}
+
 inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
 
 }  // namespace
@@ -402,8 +536,18 @@ static int resolve_proposals(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64
     int32_t *next = as<int32_t>(b.next);
     int32_t *ja = as<int32_t>(b.jmp_a), *ma = as<int32_t>(b.mx_a);
     int32_t *jb = as<int32_t>(b.jmp_b), *mb = as<int32_t>(b.mx_b);
-    CUSCAN_KERNEL(dbl_init_kernel, blocks(n), 256, 0, s, next, active_label, n, ja, ma);
     const int steps = log2_ceil(active > 1 ? active : 2) + 1;
+    if (n <= SMALL_RESOLVE_ROWS) {
+        CUSCAN_KERNEL(resolve_small_kernel, 1, SCAN_THREADS, 0, s, next, active_label,
+                      point_label, n, steps, ja, ma, jb, mb, as<int32_t>(b.keep),
+                      as<int32_t>(b.pos), as<int32_t>(b.kept_total), as<uint32_t>(b.esrc),
+                      as<uint32_t>(b.edst), as<float>(b.ew), as<int32_t>(b.parent),
+                      as<int32_t>(b.minlab), b.status, out_src, out_dst, out_w, n - 1,
+                      require_progress);
+        CUSCAN_LAUNCH(ctx, "resolve_small_kernel");
+        return CUSCAN_OK;
+    }
+    CUSCAN_KERNEL(dbl_init_kernel, blocks(n), 256, 0, s, next, active_label, n, ja, ma);
     for (int t = 0; t < steps; ++t) {
         CUSCAN_KERNEL(dbl_step_kernel, blocks(n), 256, 0, s, ja, ma, active_label, n, jb, mb);
         int32_t *tj = ja, *tm = ma;
@@ -434,14 +578,15 @@ static int resolve_proposals(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64
 
 int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int32_t *ids,
                 const float *dsq, int64_t n, int k, int32_t *label, uint32_t *out_src,
-                uint32_t *out_dst, float *out_w, cudaStream_t s) {
+                uint32_t *out_dst, float *out_w, cudaStream_t s, int64_t active_bound) {
     CUSCAN_KERNEL(seed_kernel, blocks(n), 256, 0, s, core, ids, dsq, n, k, as<int32_t>(b.next),
                                            as<uint32_t>(b.esrc), as<uint32_t>(b.edst),
                                            as<float>(b.ew), b.status);
     CUSCAN_KERNEL(iota_kernel, blocks(n), 256, 0, s, label, n);
     CUSCAN_LAUNCH(ctx, "seed_kernel");
     // all points are active nodes of the seed graph (active_label == nullptr)
-    int rc = resolve_proposals(ctx, b, n, n, nullptr, label, out_src, out_dst, out_w, 0, s);
+    int rc = resolve_proposals(ctx, b, n, active_bound > 0 ? active_bound : n, nullptr, label,
+                               out_src, out_dst, out_w, 0, s);
     if (rc) return rc;
     return CUSCAN_OK;
 }

@@ -71,10 +71,11 @@ int forest_buffers(ForestBuffers &b, Buffer **out);
 int forest_core(cuscan_ctx *ctx, const float *knn_sq, int64_t n, int k, int min_samples,
                 float *core, cudaStream_t s);
 // Seed forest (mst.rs:368-420): appends the kept seed edges and labels points by the smallest
-// point of their tree; status->components is refreshed.
+// point of their tree; status->components is refreshed. active_bound (default n) bounds the
+// nodes of the seed graph for the pointer-doubling step count.
 int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int32_t *ids,
                 const float *dsq, int64_t n, int k, int32_t *label, uint32_t *out_src,
-                uint32_t *out_dst, float *out_w, cudaStream_t s);
+                uint32_t *out_dst, float *out_w, cudaStream_t s, int64_t active_bound = -1);
 // Group points by label: perm, xp, corep, labp.
 int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, const float *core,
                              const int32_t *label, int64_t n, int d, cudaStream_t s);

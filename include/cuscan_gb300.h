@@ -240,6 +240,13 @@ typedef struct cuscan_fit_item {
     cuscan_fit_stats stats; /* out */
 } cuscan_fit_item;
 int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, int32_t count);
+/*
+ * How the context's packed fits reached their graphs so far (no reference counterpart): packs
+ * whose graph was instantiated, and packs that updated the graph instantiated for an earlier
+ * pack of the same size in place. Either pointer may be NULL.
+ */
+int cuscan_fit_core_packed_graph_stats(cuscan_ctx *ctx, int64_t *instantiations,
+                                       int64_t *updates);
 
 /*
  * Per Borůvka round of the context's last fit (no reference counterpart; the reference logs

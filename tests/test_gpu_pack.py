@@ -64,6 +64,28 @@ def test_consecutive_packs_reuse_the_workspace(gpu_ctx):
             assert_fit_equal(got, O.fit_core(x, ms))
 
 
+def test_packs_of_one_size_update_one_instantiated_graph():
+    """Packs of the same size share one graph topology: the first is instantiated, the later
+    ones (other row counts, dimensions and point sets) update it in place, and every result
+    still equals the oracle. Row counts stay above 256, where the exact kNN always splits the
+    reference range (at most 256 rows take the unsplit launch, another topology, and such a pack
+    is instantiated anew)."""
+    ctx = _lib.Context(0)
+    rng = np.random.default_rng(9)
+    rounds = 4
+    for r in range(rounds):
+        fits = [(synthetic.blobs_with_noise(n=int(rng.integers(300, 2048)),
+                                            d=int(rng.choice([8, 32, 64])),
+                                            centers=int(rng.integers(2, 20)),
+                                            seed=int(rng.integers(1 << 30))), 5,
+                 _lib.PRECISION_FP16_REFINED) for _ in range(3)]
+        packed = ctx.fit_core_packed(fits)
+        for (x, ms, _), got in zip(fits, packed):
+            assert_fit_equal(got, O.fit_core(x, ms))
+    st = ctx.packed_graph_stats()
+    assert st == {"instantiations": 1, "updates": rounds - 1}, st
+
+
 def test_pack_limits(gpu_ctx):
     x = np.zeros((2048, 4), np.float32)
     with pytest.raises(ValueError):
