@@ -18,6 +18,10 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
                               const int32_t *knn_ids, const float *knn_sq, int k,
                               const float *core, const int32_t *label, cudaStream_t s,
                               int64_t *fallback_rows);
+int launch_candidates_exact_rows(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
+                                 const int32_t *knn_ids, const float *knn_sq, int k,
+                                 const float *core, const int32_t *label, cudaStream_t s,
+                                 int64_t *screened_rows);
 int debug_screen_tile(cuscan_ctx *ctx, ForestBuffers &b, const float *x, int64_t n, int d,
                       int operands, float *out, float *rows_out, float *chunk_out,
                       float *scale_out, cudaStream_t s);
@@ -140,6 +144,8 @@ int64_t cuscan_fit_workspace_bytes(int64_t n, int32_t d, int32_t min_samples, in
     b += 8 * k * 128 * (size_t)(2 * 2 * kSMs + ceil_div(n, 128));
     if (precision == CUSCAN_PRECISION_BF16_REFINED || precision == CUSCAN_PRECISION_FP16_REFINED)
         b += refined_workspace_bytes(n, d, (int)k);
+    else if (n >= 2048)  // exact rounds over a row subset: bounds, flags, positions, counts
+        b += 7 * 4 * N + 64;
     return (int64_t)b + (1 << 20);
 }
 
@@ -298,6 +304,9 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
     int64_t rounds = 0;
     double cand_ms = 0.0, cross_pairs = 0.0;
     f->round_count = 0;
+    // exact rounds of fits of at least 2048 rows scan only the rows that can hold their
+    // component's cheapest edge (smaller fits scan every row: one host read per round fewer)
+    const bool exact_rows = !refined && n >= 2048;
     while (components > 1) {
         const int64_t rows0 = b.refined.screened_rows, tiles0 = b.refined.tile_pairs;
         if (rounds > 64) return fail(ctx, CUSCAN_NUMERICAL, "Boruvka did not converge");
@@ -308,6 +317,9 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if (refined)
             rc = launch_candidates_refined(ctx, b, n, d, knn_ids, knn_sq, k, core_sq, label, s,
                                            &boruvka_fallback_rows);
+        else if (exact_rows)
+            rc = launch_candidates_exact_rows(ctx, b, n, d, knn_ids, knn_sq, k, core_sq, label, s,
+                                              &b.refined.screened_rows);
         else
             rc = launch_candidates_fp32(ctx, as<float>(b.xp), as<float>(b.corep),
                                         as<int32_t>(b.labp), as<int32_t>(b.perm), n, d, row_keys,
@@ -315,14 +327,14 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
         if (rc) return rc;
         CUSCAN_CUDA(ctx, cudaEventRecord(ev[5], s));
         if ((rc = forest_round(ctx, b, n, components, label, mst_src, mst_dst, mst_wsq, s,
-                               refined)))
+                               refined || exact_rows)))
             return rc;
         if ((rc = read_status(ctx, b.status, hs, s))) return rc;
         cand_ms += elapsed(ev[4], ev[5]);
         cross_pairs += (double)n * (double)n - hs->same_pairs;
         if (f->round_count < FitWorkspace::kMaxRoundLog) {
             const int r = f->round_count++;
-            f->round_rows[r] = refined ? b.refined.screened_rows - rows0 : n;
+            f->round_rows[r] = refined || exact_rows ? b.refined.screened_rows - rows0 : n;
             f->round_tiles[r] = b.refined.tile_pairs - tiles0;
             f->round_ms[r] = elapsed(ev[4], ev[5]);
             f->round_cross[r] = (double)n * (double)n - hs->same_pairs;

@@ -1242,14 +1242,38 @@ __global__ void rerank_knn_kernel(const float *__restrict__ x, const int32_t *__
     for (int f = lane; f < d; f += 32) q_s[f] = x[row * d + f];
     __syncwarp();
     constexpr int W = 2 * M;  // two lists of M per row (one per column half)
-    constexpr int PER = (W + 31) / 32;
-    unsigned long long key[PER];
-#pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int s = q * 32 + lane;
-        const int32_t j = s < W ? cand_ids[row * W + s] : -1;
+    // Each half's list is sorted by lower bound. The first round takes the F smallest bounds of
+    // both lists (lanes 0..15: half 0, lanes 16..31: half 1); the rest, R per half, run in a
+    // second round only when the smaller of their two first bounds does not exceed the k-th
+    // distance of the first round, an upper bound of the final k-th distance: a candidate whose
+    // lower bound exceeds it cannot be among the row's k nearest.
+    constexpr int F = M < 16 ? M : 16;
+    constexpr int R = M - F;
+    static_assert(R <= 16, "two rounds of at most 16 candidates per half");
+    constexpr int PER = 2;
+    unsigned long long key[PER] = {~0ull, ~0ull};
+    auto round_key = [&](int first, int count) -> unsigned long long {
+        const int h = lane >> 4, o = lane & 15;
+        const int32_t j = o < count ? cand_ids[row * W + h * M + first + o] : -1;
         const float dd = staged_d2(x, d, q_s, j, rows_s, lane);
-        key[q] = j < 0 ? ~0ull : ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
+        return j < 0 ? ~0ull : ((unsigned long long)__float_as_uint(dd) << 32) | (uint32_t)perm[j];
+    };
+    key[0] = round_key(0, F);
+    if (R > 0) {
+        // k-th smallest key of the first round (all keys distinct: the halves hold disjoint
+        // columns)
+        unsigned long long a = key[0], kth = ~0ull;
+        for (int r = 0; r < k; ++r) {
+            kth = warp_min_u64(a);
+            if (kth == ~0ull) break;
+            if (a == kth) a = ~0ull;
+        }
+        const float dk0 = kth == ~0ull ? CUSCAN_INF : __uint_as_float((uint32_t)(kth >> 32));
+        float lb_rest = CUSCAN_INF;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (cand_ids[row * W + h * M + F] >= 0) lb_rest = fminf(lb_rest, cand_lb[row * W + h * M + F]);
+        if (!(lb_rest > dk0)) key[1] = round_key(F, R);
     }
     const int64_t orow = perm[row];
     float dk = CUSCAN_INF;
@@ -1474,6 +1498,22 @@ __global__ void update_row_lb_kernel(const float *__restrict__ lbtmp,
     const int64_t pos = qpos ? (int64_t)qpos[q] : q;
     const int32_t orow = perm[pos];
     rowlb[orow] = fmaxf(rowlb[orow], fminf(lbtmp[2 * q], lbtmp[2 * q + 1]));
+}
+
+// Exact rounds: the weight of each scanned row's cheapest cross-component edge (the top half of
+// its candidate key) is a lower bound of its cheapest cross edge in every later round, because
+// merging components only removes cross edges. A row without a candidate keeps ~0: +inf.
+__global__ void row_lb_from_keys_kernel(const unsigned long long *__restrict__ row_keys,
+                                        const int32_t *__restrict__ qpos,
+                                        const int32_t *__restrict__ perm, int64_t nq,
+                                        float *__restrict__ rowlb) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int64_t pos = qpos ? (int64_t)qpos[q] : q;
+    const int32_t orow = perm[pos];
+    const unsigned long long key = row_keys[orow];  // keys are kept by original row
+    const float w = key == ~0ull ? CUSCAN_INF : __uint_as_float((uint32_t)(key >> 32));
+    rowlb[orow] = fmaxf(rowlb[orow], w);
 }
 
 // Positions of the flagged rows, in order (idx is the exclusive scan of the flags).
@@ -2102,6 +2142,73 @@ int launch_candidates_refined(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int 
 // The per-row terms of the bound for the debug entry point: (ps, pb, cm, m) with
 // ps = (1 - C_B) p - abs_c, pb = (1 - C_B) p, cm = C_A m, so that the screen's bound of entry
 // (r, c) is fmaf(-cm_r, m_c, fmaf(-2, acc_rc, pb_c) + ps_r) (screen units).
+// An exact (plain f32) Borůvka round over the rows that can hold their component's cheapest
+// edge. The rows are chosen as in the screened rounds: every component gets an upper bound of
+// its cheapest cross edge from the kNN pairs (seed_bounds_kernel), and a row is skipped when its
+// core distance or its lower bound from earlier rounds exceeds that bound. Every cross edge of a
+// skipped row then weighs strictly more than the component's cheapest, so the round's winners
+// (crates/hdbscan/src/kernels/boruvka.rs:68-140 over all rows) are unchanged. The rows scanned
+// leave their exact cheapest cross edge as their lower bound for the next round.
+int launch_candidates_exact_rows(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int d,
+                                 const int32_t *knn_ids, const float *knn_sq, int k,
+                                 const float *core, const int32_t *label, cudaStream_t s,
+                                 int64_t *screened_rows) {
+    const float *xp = as<float>(b.xp);
+    const float *corep = as<float>(b.corep);
+    const int32_t *labp = as<int32_t>(b.labp);
+    const int32_t *perm = as<int32_t>(b.perm);
+    unsigned long long *row_keys = as<unsigned long long>(b.row_keys);
+    int32_t *clo = as<int32_t>(b.tile_lo), *chi = as<int32_t>(b.tile_hi);
+    RefinedBuffers &R = b.refined;
+    int rc = ensure(ctx, R.cbound, sizeof(uint32_t) * n, "component bounds");
+    if (!rc) rc = ensure(ctx, R.urow, sizeof(uint32_t) * n, "row bounds");
+    if (!rc) rc = ensure(ctx, R.count, 16, "row counts");
+    if (!rc) rc = ensure(ctx, R.act_flag, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.act_idx, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.act_pos, sizeof(int32_t) * n, "active rows");
+    if (!rc) rc = ensure(ctx, R.rowlb, sizeof(float) * n, "row lower bounds");
+    if (rc) return rc;
+    if (!R.lb_valid) {  // first round of the fit: no bounds yet
+        CUSCAN_CUDA(ctx, cudaMemsetAsync(R.rowlb.ptr, 0, sizeof(float) * n, s));
+        R.lb_valid = true;
+    }
+    CUSCAN_KERNEL(fill_u32_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, as<uint32_t>(R.cbound), n,
+                  0x7f800000u);
+    CUSCAN_KERNEL(seed_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s, knn_ids, knn_sq, k,
+                  core, label, n, as<uint32_t>(R.cbound));
+    CUSCAN_CUDA(ctx, cudaMemsetAsync(R.count.ptr, 0, 2 * sizeof(int), s));
+    CUSCAN_KERNEL(init_row_bounds_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
+                  as<uint32_t>(R.cbound), labp, corep, as<float>(R.rowlb), perm, n,
+                  as<uint32_t>(R.urow), as<int>(R.count), as<int32_t>(R.act_flag));
+    CUSCAN_LAUNCH(ctx, "component bounds");
+    if ((rc = scan_exclusive(ctx, as<int32_t>(R.act_flag), as<int32_t>(R.act_idx), n,
+                             as<int32_t>(R.count) + 1, b.scan_tmp, s)))
+        return rc;
+    int counts[2] = {0, 0};  // rows without a component bound, rows that can hold an edge
+    CUSCAN_CUDA(ctx, cudaMemcpyAsync(counts, R.count.ptr, sizeof(counts), cudaMemcpyDeviceToHost, s));
+    CUSCAN_CUDA(ctx, cudaStreamSynchronize(s));
+    const int64_t active = counts[1];
+    const int32_t *qpos = nullptr;
+    if (active == n) {
+        rc = launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s);
+    } else if (active > 0) {
+        CUSCAN_KERNEL(compact_positions_kernel, (unsigned)ceil_div(n, 256), 256, 0, s,
+                      as<int32_t>(R.act_flag), as<int32_t>(R.act_idx), n, as<int32_t>(R.act_pos));
+        CUSCAN_LAUNCH(ctx, "compact_positions_kernel");
+        qpos = as<int32_t>(R.act_pos);
+        rc = launch_candidates_fp32(ctx, xp, corep, labp, perm, n, d, row_keys, clo, chi, s, qpos,
+                                    active);
+    }
+    if (rc) return rc;
+    if (active > 0) {
+        CUSCAN_KERNEL(row_lb_from_keys_kernel, (unsigned)ceil_div(active, 256), 256, 0, s, row_keys,
+                      qpos, perm, active, as<float>(R.rowlb));
+        CUSCAN_LAUNCH(ctx, "row_lb_from_keys_kernel");
+    }
+    if (screened_rows) *screened_rows += active;
+    return CUSCAN_OK;
+}
+
 __global__ void debug_rows_kernel(const float *__restrict__ pnorm, const float *__restrict__ mnorm,
                                   int64_t n, float one_minus_cb, float abs_c, float c_a,
                                   float *__restrict__ rows) {
