@@ -349,6 +349,9 @@ int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const
         return fail(ctx, CUSCAN_CAPACITY,
                     "feature count %d exceeds the shared-memory staging limit of the kNN kernel "
                     "(at most 256 features)", d);
+    if (k == 1)  // nearest row only (the cell assignment of the bf16-refined fits)
+        return run_knn<1>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared, ids,
+                          dist, s, scratch_ids, scratch_dist, qmap);
     if (k <= 8)
         return run_knn<8>(ctx, query, nq, ref, nr, d, k, exclude_self, query_offset, squared, ids,
                           dist, s, scratch_ids, scratch_dist, qmap);

@@ -43,7 +43,8 @@ def bits(a):
 
 @pytest.mark.parametrize("n,d,k,seed", [(1, 3, 1, 0), (2, 2, 3, 1), (37, 3, 5, 2),
                                         (300, 10, 8, 3), (1000, 64, 10, 4), (2050, 128, 15, 5),
-                                        (700, 17, 16, 6), (513, 33, 32, 7), (400, 9, 40, 8)])
+                                        (700, 17, 16, 6), (513, 33, 32, 7), (400, 9, 40, 8),
+                                        (3000, 20, 1, 9)])
 def test_exact_knn_matches_oracle(gpu_ctx, n, d, k, seed):
     rng = np.random.default_rng(seed)
     x = rng.normal(size=(n, d)).astype(np.float32)
