@@ -280,6 +280,26 @@ __global__ void gather_kernel(const float *__restrict__ x, const float *__restri
 
 // Per-component minimum of (row weight bits << 32 | row) over component-sorted positions:
 // segmented warp reduction over the contiguous label runs, one atomic per run.
+// Component key of the row at sorted position pos: (weight bits << 32 | row), ~0 for a row
+// without a candidate (an error unless allow_empty) or with a non-finite weight (an error).
+__device__ __forceinline__ unsigned long long comp_key_at(int64_t pos,
+                                                          const int32_t *__restrict__ perm,
+                                                          const unsigned long long *__restrict__ row_keys,
+                                                          DevStatus *status, int allow_empty) {
+    const int32_t i = perm[pos];
+    const unsigned long long rk = row_keys[i];
+    if (rk == ~0ull) {
+        if (!allow_empty) atomicCAS(&status->err_kind, 0, 4);
+        return ~0ull;
+    }
+    const uint32_t wb = (uint32_t)(rk >> 32);
+    if (numerical_bits(wb)) {
+        atomicCAS(&status->err_kind, 0, 1);
+        return ~0ull;
+    }
+    return ((unsigned long long)wb << 32) | (uint32_t)i;
+}
+
 __global__ void component_min_kernel(const int32_t *__restrict__ perm,
                                      const int32_t *__restrict__ labp,
                                      const unsigned long long *__restrict__ row_keys, int64_t n,
@@ -290,19 +310,8 @@ __global__ void component_min_kernel(const int32_t *__restrict__ perm,
     int32_t l = -1;
     unsigned long long v = ~0ull;
     if (pos < n) {
-        int32_t i = perm[pos];
         l = labp[pos];
-        unsigned long long rk = row_keys[i];
-        if (rk == ~0ull) {
-            if (!allow_empty) atomicCAS(&status->err_kind, 0, 4);
-        } else {
-            uint32_t wb = (uint32_t)(rk >> 32);
-            if (numerical_bits(wb)) {
-                atomicCAS(&status->err_kind, 0, 1);
-            } else {
-                v = ((unsigned long long)wb << 32) | (uint32_t)i;
-            }
-        }
+        v = comp_key_at(pos, perm, row_keys, status, allow_empty);
     }
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -316,14 +325,13 @@ __global__ void component_min_kernel(const int32_t *__restrict__ perm,
 }
 
 // Winner of each active component: source = argmin row, destination = that row's candidate.
-__global__ void winner_kernel(const int32_t *__restrict__ label,
-                              const unsigned long long *__restrict__ comp_keys,
-                              const unsigned long long *__restrict__ row_keys, int64_t n,
-                              int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
-                              uint32_t *__restrict__ edst, float *__restrict__ ew,
-                              DevStatus *status) {
-    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || label[s] != (int32_t)s) return;
+__device__ __forceinline__ void winner_at(int64_t s, const int32_t *label,
+                                          const unsigned long long *__restrict__ comp_keys,
+                                          const unsigned long long *__restrict__ row_keys,
+                                          int64_t n, int32_t *__restrict__ next,
+                                          uint32_t *__restrict__ esrc, uint32_t *__restrict__ edst,
+                                          float *__restrict__ ew, DevStatus *status) {
+    if (label[s] != (int32_t)s) return;
     unsigned long long ck = comp_keys[s];
     if (ck == ~0ull) {
         atomicCAS(&status->err_kind, 0, 4);
@@ -341,6 +349,16 @@ __global__ void winner_kernel(const int32_t *__restrict__ label,
     esrc[s] = src;
     edst[s] = dst;
     ew[s] = __uint_as_float((uint32_t)(ck >> 32));
+}
+
+__global__ void winner_kernel(const int32_t *__restrict__ label,
+                              const unsigned long long *__restrict__ comp_keys,
+                              const unsigned long long *__restrict__ row_keys, int64_t n,
+                              int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
+                              uint32_t *__restrict__ edst, float *__restrict__ ew,
+                              DevStatus *status) {
+    int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) winner_at(s, label, comp_keys, row_keys, n, next, esrc, edst, ew, status);
 }
 
 // ---- exclusive scan of int32 (three passes) ----
@@ -423,16 +441,14 @@ __global__ void scan_add_kernel(int32_t *__restrict__ out, int64_t n,
 // active_label and point_label are the same array (no __restrict__ on either).
 constexpr int64_t SMALL_RESOLVE_ROWS = 2048;
 constexpr int SMALL_ITEMS = (int)(SMALL_RESOLVE_ROWS / SCAN_THREADS);
-__global__ void __launch_bounds__(SCAN_THREADS)
-    resolve_small_kernel(const int32_t *__restrict__ next, const int32_t *active_label,
-                         int32_t *point_label, int64_t n, int steps, int32_t *ja,
-                         int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
-                         int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
-                         const uint32_t *__restrict__ esrc, const uint32_t *__restrict__ edst,
-                         const float *__restrict__ ew, int32_t *parent,
-                         int32_t *__restrict__ minlab, DevStatus *status,
-                         uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
-                         float *__restrict__ out_w, int64_t capacity, int require_progress) {
+__device__ __forceinline__ void resolve_block(
+    const int32_t *__restrict__ next, const int32_t *active_label, int32_t *point_label, int64_t n,
+    int steps, int32_t *ja, int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
+    int32_t *__restrict__ pos, int32_t *__restrict__ kept_total, const uint32_t *__restrict__ esrc,
+    const uint32_t *__restrict__ edst, const float *__restrict__ ew, int32_t *parent,
+    int32_t *__restrict__ minlab, DevStatus *status, uint32_t *__restrict__ out_src,
+    uint32_t *__restrict__ out_dst, float *__restrict__ out_w, int64_t capacity,
+    int require_progress) {
     __shared__ int warp_sums[SCAN_THREADS / 32];
     const int tid = threadIdx.x;
     // cycle breaking: pointer doubling with a running maximum, ping-pong buffers
@@ -496,6 +512,103 @@ __global__ void __launch_bounds__(SCAN_THREADS)
         roots += __syncthreads_count(i < n && point_label[i] == (int32_t)i);
     }
     if (tid == 0) status->components = (unsigned long long)roots;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    resolve_small_kernel(const int32_t *__restrict__ next, const int32_t *active_label,
+                         int32_t *point_label, int64_t n, int steps, int32_t *ja,
+                         int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
+                         int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
+                         const uint32_t *__restrict__ esrc, const uint32_t *__restrict__ edst,
+                         const float *__restrict__ ew, int32_t *parent,
+                         int32_t *__restrict__ minlab, DevStatus *status,
+                         uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
+                         float *__restrict__ out_w, int64_t capacity, int require_progress) {
+    resolve_block(next, active_label, point_label, n, steps, ja, ma, jb, mb, keep, pos, kept_total,
+                  esrc, edst, ew, parent, minlab, status, out_src, out_dst, out_w, capacity,
+                  require_progress);
+}
+
+// A Borůvka round's winners and merge for at most SMALL_RESOLVE_ROWS points in one CTA: the
+// per-component minimum key (component_min_kernel's keys, reduced with block atomics), the
+// winners (winner_kernel), then resolve_block. One launch instead of four.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    round_small_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ labp,
+                       const unsigned long long *__restrict__ row_keys,
+                       unsigned long long *__restrict__ comp_keys, int allow_empty,
+                       int32_t *label, int64_t n, int steps, int32_t *next, int32_t *ja,
+                       int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
+                       int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
+                       uint32_t *esrc, uint32_t *edst, float *ew, int32_t *parent,
+                       int32_t *__restrict__ minlab, DevStatus *status,
+                       uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
+                       float *__restrict__ out_w, int64_t capacity) {
+    const int tid = threadIdx.x;
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) comp_keys[i] = ~0ull;
+    __syncthreads();
+    for (int64_t p = tid; p < n; p += SCAN_THREADS) {
+        const unsigned long long v = comp_key_at(p, perm, row_keys, status, allow_empty);
+        if (v != ~0ull) atomicMin(&comp_keys[labp[p]], v);
+    }
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += SCAN_THREADS)
+        winner_at(i, label, comp_keys, row_keys, n, next, esrc, edst, ew, status);
+    __syncthreads();
+    resolve_block(next, label, label, n, steps, ja, ma, jb, mb, keep, pos, kept_total, esrc, edst,
+                  ew, parent, minlab, status, out_src, out_dst, out_w, capacity, 1);
+}
+
+// Counting sort by label for at most SMALL_RESOLVE_ROWS points in one CTA: histogram, sum of
+// squared sizes, exclusive scan and scatter (hist_kernel, same_pairs_kernel, scan_exclusive,
+// scatter_kernel). The order of points within a label is free, as in scatter_kernel.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    sort_small_kernel(const int32_t *__restrict__ label, int64_t n, int32_t *__restrict__ cnt,
+                      int32_t *__restrict__ start, int32_t *__restrict__ fill,
+                      int32_t *__restrict__ perm, DevStatus *status) {
+    __shared__ int warp_sums[SCAN_THREADS / 32];
+    __shared__ double pair_sums[SCAN_THREADS / 32];
+    const int tid = threadIdx.x;
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) {
+        cnt[i] = 0;
+        fill[i] = 0;
+    }
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) atomicAdd(&cnt[label[i]], 1);
+    __syncthreads();
+    // sum of squared sizes (exact in f64: integers below 2^53)
+    double v = 0.0;
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) {
+        const double c = (double)cnt[i];
+        v += c * c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) pair_sums[tid >> 5] = v;
+    int c[SMALL_ITEMS];
+    int sum = 0;
+    const int64_t base = (int64_t)tid * SMALL_ITEMS;
+#pragma unroll
+    for (int u = 0; u < SMALL_ITEMS; ++u) {
+        c[u] = base + u < n ? cnt[base + u] : 0;
+        sum += c[u];
+    }
+    int total;
+    int prefix = block_exclusive_scan(sum, warp_sums, total);
+#pragma unroll
+    for (int u = 0; u < SMALL_ITEMS; ++u) {
+        if (base + u < n) start[base + u] = prefix;
+        prefix += c[u];
+    }
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < SCAN_THREADS / 32; ++w) t += pair_sums[w];
+        status->same_pairs = t;
+    }
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) {
+        const int32_t l = label[i];
+        perm[start[l] + atomicAdd(&fill[l], 1)] = (int32_t)i;
+    }
 }
 
 inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
@@ -594,6 +707,14 @@ int forest_seed(cuscan_ctx *ctx, ForestBuffers &b, const float *core, const int3
 int forest_sort_by_component(cuscan_ctx *ctx, ForestBuffers &b, const float *x, const float *core,
                              const int32_t *label, int64_t n, int d, cudaStream_t s) {
     int32_t *cnt = as<int32_t>(b.cnt), *start = as<int32_t>(b.start), *fill = as<int32_t>(b.fill);
+    if (n <= SMALL_RESOLVE_ROWS) {
+        CUSCAN_KERNEL(sort_small_kernel, 1, SCAN_THREADS, 0, s, label, n, cnt, start, fill,
+                      as<int32_t>(b.perm), b.status);
+        CUSCAN_KERNEL(gather_kernel, blocks(n * d), 256, 0, s, x, core, label, as<int32_t>(b.perm),
+                      n, d, as<float>(b.xp), as<float>(b.corep), as<int32_t>(b.labp));
+        CUSCAN_LAUNCH(ctx, "component sort");
+        return CUSCAN_OK;
+    }
     CUSCAN_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * n, s));
     CUSCAN_CUDA(ctx, cudaMemsetAsync(fill, 0, sizeof(int32_t) * n, s));
     CUSCAN_KERNEL(hist_kernel, blocks(n), 256, 0, s, label, n, cnt);
@@ -614,6 +735,19 @@ int forest_round(cuscan_ctx *ctx, ForestBuffers &b, int64_t n, int64_t component
                  int32_t *label, uint32_t *out_src, uint32_t *out_dst, float *out_w,
                  cudaStream_t s, int allow_empty) {
     unsigned long long *comp_keys = as<unsigned long long>(b.comp_keys);
+    if (n <= SMALL_RESOLVE_ROWS) {
+        const int steps = log2_ceil(components > 1 ? components : 2) + 1;
+        CUSCAN_KERNEL(round_small_kernel, 1, SCAN_THREADS, 0, s, as<int32_t>(b.perm),
+                      as<int32_t>(b.labp), as<unsigned long long>(b.row_keys), comp_keys,
+                      allow_empty, label, n, steps, as<int32_t>(b.next), as<int32_t>(b.jmp_a),
+                      as<int32_t>(b.mx_a), as<int32_t>(b.jmp_b), as<int32_t>(b.mx_b),
+                      as<int32_t>(b.keep), as<int32_t>(b.pos), as<int32_t>(b.kept_total),
+                      as<uint32_t>(b.esrc), as<uint32_t>(b.edst), as<float>(b.ew),
+                      as<int32_t>(b.parent), as<int32_t>(b.minlab), b.status, out_src, out_dst,
+                      out_w, n - 1);
+        CUSCAN_LAUNCH(ctx, "round_small_kernel");
+        return CUSCAN_OK;
+    }
     int rc = launch_fill_u64(ctx, comp_keys, n, ~0ull, s);
     if (rc) return rc;
     CUSCAN_KERNEL(component_min_kernel, blocks(n), 256, 0, s, as<int32_t>(b.perm),
