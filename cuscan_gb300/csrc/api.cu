@@ -166,9 +166,27 @@ int cuscan_exact_knn(cuscan_ctx *ctx, const float *query, int64_t nq, const floa
     if (nq > 0 && (!query || !reference || !ids_out || !dist_out))
         return fail(ctx, CUSCAN_INVALID_INPUT, "exact_knn received a null pointer");
     CUSCAN_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = pick_stream(ctx, stream);
+    // The kNN of a point set against itself (the fit's core-distance sweep) takes the tensor-core
+    // screen with exact re-rank, whose rows equal the exact sweep's bit for bit; it falls back to
+    // the exact sweep itself for shapes outside the screen's tiling (fewer than 2048 rows,
+    // k > 32, more than 128 features, values that overflow f32).
+    if (query == reference && nq == nr && query_offset == 0 && exclude_self && squared &&
+        nr >= 2048 && k <= 32 && refined_available()) {
+        ForestBuffers &b = ctx->fit->forest;
+        int rc = forest_reserve(ctx, b, nr, d);
+        if (rc) return rc;
+        b.refined.want_fp16 = false;
+        b.refined.have_scale = false;
+        b.refined.split = false;
+        b.refined.screen_timed = false;
+        int64_t refined_rows = 0, fallback_rows = 0, rescreened_rows = 0;
+        return launch_knn_refined(ctx, b, reference, nr, d, k, ids_out, dist_out, s, &refined_rows,
+                                  &fallback_rows, &rescreened_rows);
+    }
     return launch_exact_knn_fp32(ctx, query, nq, reference, nr, d, k, exclude_self, query_offset,
-                                 squared, ids_out, dist_out, pick_stream(ctx, stream),
-                                 ctx->fit->op_knn_ids, ctx->fit->op_knn_dist);
+                                 squared, ids_out, dist_out, s, ctx->fit->op_knn_ids,
+                                 ctx->fit->op_knn_dist);
 }
 
 int cuscan_boruvka_candidates(cuscan_ctx *ctx, const float *data, const float *core_sq,

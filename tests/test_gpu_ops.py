@@ -54,6 +54,28 @@ def test_exact_knn_matches_oracle(gpu_ctx, n, d, k, seed):
     np.testing.assert_array_equal(bits(ds), bits(eds))
 
 
+def _self_knn_sets():
+    from cuscan_gb300 import synthetic
+
+    yield "vmf_6k_d128", synthetic.vmf_like(n=6000, d=128, seed=3), 15
+    yield "blobs_far_5k_d64", (synthetic.blobs_with_noise(n=5000, d=64, seed=4) + 200.0).astype(
+        np.float32), 10
+    yield "normal_4k_d20_k1", np.random.default_rng(5).normal(size=(4000, 20)).astype(np.float32), 1
+    yield "normal_3k_d33_k32", np.random.default_rng(6).normal(size=(3000, 33)).astype(np.float32), 32
+
+
+@pytest.mark.parametrize("name,x,k", list(_self_knn_sets()), ids=lambda v: v if isinstance(v, str) else "")
+def test_exact_knn_of_a_set_against_itself_takes_the_screen_and_stays_exact(gpu_ctx, name, x, k):
+    """From 2048 rows the kNN of a point set against itself runs the tensor-core screen with
+    exact re-rank (falling back to the exact sweep where the screen cannot decide); its ids and
+    squared distances equal the oracle's bit for bit, including far-from-origin data that needs
+    the tightened operands."""
+    ids, ds = gpu_knn(gpu_ctx, x, x, k)
+    eids, eds = O.exact_neighbors(x, x, k)
+    np.testing.assert_array_equal(ids, eids)
+    np.testing.assert_array_equal(bits(ds), bits(eds))
+
+
 def test_exact_knn_ties_duplicates_and_lattice(gpu_ctx):
     rng = np.random.default_rng(11)
     base = rng.integers(0, 4, size=(300, 3)).astype(np.float32)   # many exact ties
