@@ -404,3 +404,25 @@ def test_fit_core_into_caller_outputs(gpu_ctx):
     assert got["core_sq"] is out["core_sq"]
     with pytest.raises(ValueError):
         gpu_ctx.fit_core(x, 5, out=gpu_ctx.fit_core_outputs(2999, 5))
+
+
+@pytest.mark.parametrize("precision", [_lib.PRECISION_PLAIN, _lib.PRECISION_BF16_REFINED])
+def test_round_stats_and_row_selection(gpu_ctx, precision):
+    """cuscan_fit_round_stats reports one entry per Borůvka round of the last fit. From 2048
+    rows both the screened and the exact rounds scan only the rows that can hold their
+    component's cheapest edge: the per-round rows add up to boruvka_screened_rows, stay within
+    n, fall below n in a later round, and the fit still equals the oracle."""
+    x = synthetic.blobs_with_noise(n=20_000, d=16, centers=40, seed=12)
+    got = gpu_ctx.fit_core(x, 5, precision)
+    assert_fit_equal(got, O.fit_core(x, 5))
+    st = got["stats"]
+    rounds = gpu_ctx.round_stats()
+    assert len(rounds) == st["rounds"] >= 2
+    rows = [r["rows"] for r in rounds]
+    assert all(0 <= r <= x.shape[0] for r in rows)
+    assert sum(rows) == st["boruvka_screened_rows"]
+    assert min(rows[1:]) < x.shape[0]
+    cross = [r["cross_pairs"] for r in rounds]
+    assert all(a >= b for a, b in zip(cross, cross[1:]))
+    if precision == _lib.PRECISION_PLAIN:
+        assert all(r["tiles"] == 0 for r in rounds)
