@@ -50,7 +50,7 @@ SIGNATURES = {
     "cuscan_fit_core_device": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                          _VP, _VP, _VP, _VP, _VP, _VP, _I64P, _VP, _VP]),
     "cuscan_fit_core_packed": (C.c_int, [_VP, _VP, C.c_int32]),
-    "cuscan_fit_core_packed_graph_stats": (C.c_int, [_VP, _I64P, _I64P]),
+    "cuscan_fit_core_packed_launch_stats": (C.c_int, [_VP, _I64P, _I64P]),
     "cuscan_debug_screen_tile": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, _VP, _VP]),
     "cuscan_debug_screen_tile_operands": (C.c_int, [_VP, _VP, C.c_int64, C.c_int32, C.c_int32,
                                                     _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
@@ -452,7 +452,7 @@ class Context:
 
 
     def fit_core_packed(self, fits):
-        """Fit cores of several small point sets in one CUDA graph launch.
+        """Fit cores of several small point sets, each step of every fit in one launch.
 
         `fits` is a sequence of (x, min_samples, precision). Returns one dict per fit, shaped
         like fit_core's, plus its "status"; raises if any fit failed (the first failure)."""
@@ -486,13 +486,13 @@ class Context:
             o["status"] = int(item.status)
         return outs
 
-    def packed_graph_stats(self) -> dict:
-        """Packs of this context whose graph was instantiated, and packs that updated the graph
-        of an earlier pack of the same size in place."""
-        inst, upd = C.c_int64(0), C.c_int64(0)
-        self.check(self._lib.cuscan_fit_core_packed_graph_stats(self.handle, C.byref(inst),
-                                                                C.byref(upd)))
-        return {"instantiations": int(inst.value), "updates": int(upd.value)}
+    def packed_launch_stats(self) -> dict:
+        """The latest pack of this context: kernels launched and host reads of its round
+        counter."""
+        launches, reads = C.c_int64(0), C.c_int64(0)
+        self.check(self._lib.cuscan_fit_core_packed_launch_stats(self.handle, C.byref(launches),
+                                                                 C.byref(reads)))
+        return {"launches": int(launches.value), "host_reads": int(reads.value)}
 
 
 def clusters_from_spanning_tree(src, dst, weight, *, min_cluster_size: int,

@@ -13,7 +13,7 @@
 // before any distance is computed; tile label ranges are precomputed per 32-row tile.
 #include <mutex>
 
-#include "common.cuh"
+#include "forest.cuh"
 
 namespace cuscan {
 namespace {
@@ -72,25 +72,30 @@ __device__ __forceinline__ void load_tile(float *tile, float *core_t, int32_t *l
     }
 }
 
-__global__ void __launch_bounds__(QB) candidates_fp32_kernel(
+// Per-tile row data of the candidate sweep, double-buffered in shared memory.
+struct CandShared {
+    float core_t[2][RT];
+    int32_t lab_t[2][RT];
+    int32_t id_t[2][RT];
+    int32_t q_range[2];
+};
+
+// One block: QB query rows [q0, q0 + QB) against rows [r_begin, r_end); each query's cheapest
+// cross-component key is folded into row_keys with atomicMin.
+__device__ __forceinline__ void candidates_block(
     const float *__restrict__ data, const float *__restrict__ core,
     const int32_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n, int d,
-    const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t ref_chunk,
-    unsigned long long *__restrict__ row_keys, const int32_t *__restrict__ qmap, int64_t nq,
-    int64_t qoff) {
-    extern __shared__ __align__(16) float smem[];
+    const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t q0,
+    int64_t r_begin, int64_t r_end, unsigned long long *__restrict__ row_keys,
+    const int32_t *__restrict__ qmap, int64_t nq, int64_t qoff, float *smem, CandShared &sh) {
     float *qs = smem;                       // [d][QB]
     float *tiles = smem + (size_t)d * QB;   // 2 x [d][RTP]
-    __shared__ float core_t[2][RT];
-    __shared__ int32_t lab_t[2][RT];
-    __shared__ int32_t id_t[2][RT];
-    __shared__ int32_t q_range[2];
+    float(&core_t)[2][RT] = sh.core_t;
+    int32_t(&lab_t)[2][RT] = sh.lab_t;
+    int32_t(&id_t)[2][RT] = sh.id_t;
+    int32_t *q_range = sh.q_range;
     const int tid = threadIdx.x;
-    const int64_t q0 = (int64_t)blockIdx.x * QB;
     const int64_t qi = q0 + tid;
-    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
-    int64_t r_end = r_begin + ref_chunk;
-    if (r_end > n) r_end = n;
 
     // query rows are positions qmap[qi] (or qoff + qi) of the same arrays
     const bool q_valid = qi < nq;
@@ -184,6 +189,39 @@ __global__ void __launch_bounds__(QB) candidates_fp32_kernel(
         const int32_t out = ids ? ids[qpos] : (int32_t)qpos;
         atomicMin(&row_keys[out], best);
     }
+}
+
+__global__ void __launch_bounds__(QB) candidates_fp32_kernel(
+    const float *__restrict__ data, const float *__restrict__ core,
+    const int32_t *__restrict__ labels, const int32_t *__restrict__ ids, int64_t n, int d,
+    const int32_t *__restrict__ tile_lo, const int32_t *__restrict__ tile_hi, int64_t ref_chunk,
+    unsigned long long *__restrict__ row_keys, const int32_t *__restrict__ qmap, int64_t nq,
+    int64_t qoff) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ CandShared sh;
+    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
+    int64_t r_end = r_begin + ref_chunk;
+    if (r_end > n) r_end = n;
+    candidates_block(data, core, labels, ids, n, d, tile_lo, tile_hi, (int64_t)blockIdx.x * QB,
+                     r_begin, r_end, row_keys, qmap, nq, qoff, smem, sh);
+}
+
+// Packed fits: fit blockIdx.z (skipped unless its round runs), query block blockIdx.x,
+// reference chunk blockIdx.y of `splits`, over the fit's component-sorted copies (the launch
+// launch_candidates_fp32 makes for a fit alone).
+__global__ void __launch_bounds__(QB) pack_candidates_kernel(const PackFit *__restrict__ fits,
+                                                             int splits) {
+    extern __shared__ __align__(16) float smem[];
+    __shared__ CandShared sh;
+    const PackFit &f = fits[blockIdx.z];
+    const int64_t n = f.n, q0 = (int64_t)blockIdx.x * QB;
+    if (q0 >= n || !*(volatile int32_t *)&f.kept_total[1]) return;
+    const int64_t chunk = ceil_div(ceil_div(n, (int64_t)splits), (int64_t)RT) * RT;
+    const int64_t r_begin = (int64_t)blockIdx.y * chunk;
+    if (r_begin >= n) return;
+    const int64_t r_end = r_begin + chunk < n ? r_begin + chunk : n;
+    candidates_block(f.xp, f.corep, f.labp, f.perm, n, f.d, f.tile_lo, f.tile_hi, q0, r_begin,
+                     r_end, f.row_keys, nullptr, n, 0, smem, sh);
 }
 
 __global__ void fill_u64_kernel(unsigned long long *p, int64_t n, unsigned long long v) {
@@ -343,6 +381,19 @@ int launch_candidates_fp32(cuscan_ctx *ctx, const float *data, const float *core
     CUSCAN_KERNEL(candidates_fp32_kernel, grid, QB, smem, s, data, core_sq, labels, ids, n, d,
                   tile_lo, tile_hi, chunk, row_keys, qmap, nq, qoff);
     CUSCAN_LAUNCH(ctx, "candidates_fp32_kernel");
+    return CUSCAN_OK;
+}
+
+int launch_pack_candidates(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max,
+                           int d_max, int splits, cudaStream_t s) {
+    const size_t smem = ((size_t)d_max * QB + 2 * (size_t)d_max * RTP) * sizeof(float);
+    if (smem > 200 * 1024)
+        return fail(ctx, CUSCAN_CAPACITY, "feature count %d exceeds the Boruvka staging limit",
+                    d_max);
+    if (int rc = allow_dynamic_smem(ctx, pack_candidates_kernel, smem)) return rc;
+    dim3 grid((unsigned)ceil_div(n_max, QB), (unsigned)splits, (unsigned)count);
+    CUSCAN_KERNEL(pack_candidates_kernel, grid, QB, smem, s, fits, splits);
+    CUSCAN_LAUNCH(ctx, "pack_candidates_kernel");
     return CUSCAN_OK;
 }
 

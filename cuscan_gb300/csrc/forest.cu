@@ -23,10 +23,8 @@ __device__ __forceinline__ bool active_node(const int32_t *label, int64_t s) {
     return label == nullptr || label[s] == (int32_t)s;
 }
 
-__global__ void core_kernel(const float *__restrict__ knn_sq, int64_t n, int k, int min_samples,
-                            float *__restrict__ core) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void core_at(int64_t i, const float *__restrict__ knn_sq, int64_t n,
+                                        int k, int min_samples, float *__restrict__ core) {
     float c;
     if ((int64_t)min_samples >= n)
         c = CUSCAN_INF;
@@ -37,15 +35,20 @@ __global__ void core_kernel(const float *__restrict__ knn_sq, int64_t n, int k, 
     core[i] = c;
 }
 
+__global__ void core_kernel(const float *__restrict__ knn_sq, int64_t n, int k, int min_samples,
+                            float *__restrict__ core) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) core_at(i, knn_sq, n, k, min_samples, core);
+}
+
 // Seed proposal of point i: the first non-padding neighbour j with core_i >= core_j
 // (mst.rs:390-417); next[i] = i when there is none.
-__global__ void seed_kernel(const float *__restrict__ core, const int32_t *__restrict__ ids,
-                            const float *__restrict__ dsq, int64_t n, int k,
-                            int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
-                            uint32_t *__restrict__ edst, float *__restrict__ ew,
-                            DevStatus *status) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void seed_at(int64_t i, const float *__restrict__ core,
+                                        const int32_t *__restrict__ ids,
+                                        const float *__restrict__ dsq, int64_t n, int k,
+                                        int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
+                                        uint32_t *__restrict__ edst, float *__restrict__ ew,
+                                        DevStatus *status) {
     const float ci = core[i];
     int32_t pick = (int32_t)i;
     float w = 0.0f;
@@ -66,6 +69,15 @@ __global__ void seed_kernel(const float *__restrict__ core, const int32_t *__res
     esrc[i] = (uint32_t)i;
     edst[i] = (uint32_t)pick;
     ew[i] = w;
+}
+
+__global__ void seed_kernel(const float *__restrict__ core, const int32_t *__restrict__ ids,
+                            const float *__restrict__ dsq, int64_t n, int k,
+                            int32_t *__restrict__ next, uint32_t *__restrict__ esrc,
+                            uint32_t *__restrict__ edst, float *__restrict__ ew,
+                            DevStatus *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) seed_at(i, core, ids, dsq, n, k, next, esrc, edst, ew, status);
 }
 
 __global__ void iota_kernel(int32_t *p, int64_t n) {
@@ -532,17 +544,14 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 // A Borůvka round's winners and merge for at most SMALL_RESOLVE_ROWS points in one CTA: the
 // per-component minimum key (component_min_kernel's keys, reduced with block atomics), the
 // winners (winner_kernel), then resolve_block. One launch instead of four.
-__global__ void __launch_bounds__(SCAN_THREADS)
-    round_small_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ labp,
-                       const unsigned long long *__restrict__ row_keys,
-                       unsigned long long *__restrict__ comp_keys, int allow_empty,
-                       int32_t *label, int64_t n, int steps, int32_t *next, int32_t *ja,
-                       int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
-                       int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
-                       uint32_t *esrc, uint32_t *edst, float *ew, int32_t *parent,
-                       int32_t *__restrict__ minlab, DevStatus *status,
-                       uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
-                       float *__restrict__ out_w, int64_t capacity) {
+__device__ __forceinline__ void round_block(
+    const int32_t *__restrict__ perm, const int32_t *__restrict__ labp,
+    const unsigned long long *__restrict__ row_keys, unsigned long long *__restrict__ comp_keys,
+    int allow_empty, int32_t *label, int64_t n, int steps, int32_t *next, int32_t *ja,
+    int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep, int32_t *__restrict__ pos,
+    int32_t *__restrict__ kept_total, uint32_t *esrc, uint32_t *edst, float *ew, int32_t *parent,
+    int32_t *__restrict__ minlab, DevStatus *status, uint32_t *__restrict__ out_src,
+    uint32_t *__restrict__ out_dst, float *__restrict__ out_w, int64_t capacity) {
     const int tid = threadIdx.x;
     for (int64_t i = tid; i < n; i += SCAN_THREADS) comp_keys[i] = ~0ull;
     __syncthreads();
@@ -558,13 +567,29 @@ __global__ void __launch_bounds__(SCAN_THREADS)
                   ew, parent, minlab, status, out_src, out_dst, out_w, capacity, 1);
 }
 
+__global__ void __launch_bounds__(SCAN_THREADS)
+    round_small_kernel(const int32_t *__restrict__ perm, const int32_t *__restrict__ labp,
+                       const unsigned long long *__restrict__ row_keys,
+                       unsigned long long *__restrict__ comp_keys, int allow_empty,
+                       int32_t *label, int64_t n, int steps, int32_t *next, int32_t *ja,
+                       int32_t *ma, int32_t *jb, int32_t *mb, int32_t *__restrict__ keep,
+                       int32_t *__restrict__ pos, int32_t *__restrict__ kept_total,
+                       uint32_t *esrc, uint32_t *edst, float *ew, int32_t *parent,
+                       int32_t *__restrict__ minlab, DevStatus *status,
+                       uint32_t *__restrict__ out_src, uint32_t *__restrict__ out_dst,
+                       float *__restrict__ out_w, int64_t capacity) {
+    round_block(perm, labp, row_keys, comp_keys, allow_empty, label, n, steps, next, ja, ma, jb,
+                mb, keep, pos, kept_total, esrc, edst, ew, parent, minlab, status, out_src,
+                out_dst, out_w, capacity);
+}
+
 // Counting sort by label for at most SMALL_RESOLVE_ROWS points in one CTA: histogram, sum of
 // squared sizes, exclusive scan and scatter (hist_kernel, same_pairs_kernel, scan_exclusive,
 // scatter_kernel). The order of points within a label is free, as in scatter_kernel.
-__global__ void __launch_bounds__(SCAN_THREADS)
-    sort_small_kernel(const int32_t *__restrict__ label, int64_t n, int32_t *__restrict__ cnt,
-                      int32_t *__restrict__ start, int32_t *__restrict__ fill,
-                      int32_t *__restrict__ perm, DevStatus *status) {
+__device__ __forceinline__ void sort_block(const int32_t *__restrict__ label, int64_t n,
+                                           int32_t *__restrict__ cnt, int32_t *__restrict__ start,
+                                           int32_t *__restrict__ fill, int32_t *__restrict__ perm,
+                                           DevStatus *status) {
     __shared__ int warp_sums[SCAN_THREADS / 32];
     __shared__ double pair_sums[SCAN_THREADS / 32];
     const int tid = threadIdx.x;
@@ -609,6 +634,13 @@ __global__ void __launch_bounds__(SCAN_THREADS)
         const int32_t l = label[i];
         perm[start[l] + atomicAdd(&fill[l], 1)] = (int32_t)i;
     }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    sort_small_kernel(const int32_t *__restrict__ label, int64_t n, int32_t *__restrict__ cnt,
+                      int32_t *__restrict__ start, int32_t *__restrict__ fill,
+                      int32_t *__restrict__ perm, DevStatus *status) {
+    sort_block(label, n, cnt, start, fill, perm, status);
 }
 
 inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)ceil_div(n > 0 ? n : 1, t); }
@@ -875,6 +907,181 @@ void forest_release(ForestBuffers &b) {
     const int count = forest_buffers(b, all);
     for (int i = 0; i < count; ++i) release(*all[i]);
     b.status = nullptr;
+}
+
+// ---- packed small fits: the one-CTA steps of every fit of a pack, one launch each ----
+namespace {
+
+constexpr int kPackRowTile = 32;  // rows per label-range tile of the candidate sweep
+
+__device__ __forceinline__ int log2_ceil_dev(int64_t c) {
+    int l = 0;
+    while ((1ll << l) < c) ++l;
+    return l;
+}
+
+// Fit blockIdx.x: core column, seed proposals, labels 0..n-1 and the seed's merge; the kernels
+// core_kernel, seed_kernel, iota_kernel and resolve_small_kernel of the fit alone, with its
+// step count. Block 0 also clears the pack's per-round counters.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    pack_seed_kernel(const PackFit *__restrict__ fits, int *more) {
+    const PackFit &f = fits[blockIdx.x];
+    const int tid = threadIdx.x;
+    const int64_t n = f.n;
+    DevStatus *st = f.status;
+    if (blockIdx.x == 0)
+        for (int r = tid; r < kPackMaxRounds + 2; r += SCAN_THREADS) more[r] = 0;
+    if (tid == 0) {
+        *st = DevStatus{};
+        f.kept_total[1] = 0;
+    }
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) core_at(i, f.dsq, n, f.k, f.min_samples, f.core);
+    __syncthreads();
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) {
+        seed_at(i, f.core, f.ids, f.dsq, n, f.k, f.next, f.esrc, f.edst, f.ew, st);
+        f.label[i] = (int32_t)i;
+    }
+    __syncthreads();
+    resolve_block(f.next, nullptr, f.label, n, log2_ceil_dev(n > 1 ? n : 2) + 1, f.ja, f.ma,
+                  f.jb, f.mb, f.keep, f.pos, f.kept_total, f.esrc, f.edst, f.ew, f.parent,
+                  f.minlab, st, f.src, f.dst, f.w, n - 1, 0);
+    if (tid == 0) {
+        st->seed_edges = st->edges;
+        st->components_after_seed = st->components;
+    }
+}
+
+// Start of round r of fit blockIdx.x: whether it runs (more than one component, no error,
+// within the round limit: the host driver's checks), then the component sort, the sorted copies
+// (gather_kernel), cleared row keys and the label range of every 32-row tile
+// (tile_range_kernel).
+__global__ void __launch_bounds__(SCAN_THREADS) pack_sort_kernel(const PackFit *__restrict__ fits) {
+    const PackFit &f = fits[blockIdx.x];
+    const int tid = threadIdx.x;
+    const int64_t n = f.n;
+    DevStatus *st = f.status;
+    __shared__ int run;
+    if (tid == 0) {
+        int on = st->components > 1 && st->err_kind == 0;
+        if (on && st->rounds > (unsigned long long)kPackMaxRounds) {
+            st->err_kind = kPackErrNoConvergence;
+            on = 0;
+        }
+        f.kept_total[1] = on;
+        run = on;
+    }
+    __syncthreads();
+    if (!run) return;
+    sort_block(f.label, n, f.cnt, f.start, f.fill, f.perm, st);
+    __syncthreads();
+    const int d = f.d;
+    for (int64_t e = tid; e < n * d; e += SCAN_THREADS) {
+        const int64_t p = e / d;
+        const int c = (int)(e - p * d);
+        const int32_t i = f.perm[p];
+        f.xp[e] = f.x[(int64_t)i * d + c];
+        if (c == 0) {
+            f.corep[p] = f.core[i];
+            f.labp[p] = f.label[i];
+        }
+    }
+    for (int64_t i = tid; i < n; i += SCAN_THREADS) f.row_keys[i] = ~0ull;
+    __syncthreads();
+    const int64_t tiles = ceil_div(n, kPackRowTile);
+    for (int64_t t = tid; t < tiles; t += SCAN_THREADS) {
+        const int64_t a = t * kPackRowTile, b = a + kPackRowTile < n ? a + kPackRowTile : n;
+        int32_t mn = f.labp[a], mx = mn;
+        for (int64_t i = a + 1; i < b; ++i) {
+            const int32_t l = f.labp[i];
+            mn = l < mn ? l : mn;
+            mx = l > mx ? l : mx;
+        }
+        f.tile_lo[t] = mn;
+        f.tile_hi[t] = mx;
+    }
+}
+
+// End of round r of fit blockIdx.x: winners and merge (round_small_kernel), then the round's
+// bookkeeping (rounds run, ordered cross pairs entering it) and whether another round is due.
+__global__ void __launch_bounds__(SCAN_THREADS)
+    pack_merge_kernel(const PackFit *__restrict__ fits, int r, int *more) {
+    const PackFit &f = fits[blockIdx.x];
+    if (!*(volatile int32_t *)&f.kept_total[1]) return;
+    const int tid = threadIdx.x;
+    const int64_t n = f.n;
+    DevStatus *st = f.status;
+    const int64_t comps = (int64_t)st->components;
+    __syncthreads();  // every thread has the count before the merge rewrites it
+    round_block(f.perm, f.labp, f.row_keys, f.comp_keys, f.allow_empty, f.label, n,
+                log2_ceil_dev(comps > 1 ? comps : 2) + 1, f.next, f.ja, f.ma, f.jb, f.mb, f.keep,
+                f.pos, f.kept_total, f.esrc, f.edst, f.ew, f.parent, f.minlab, st, f.src, f.dst,
+                f.w, n - 1);
+    if (tid == 0) {
+        st->rounds += 1;
+        st->cross_pairs += (double)n * (double)n - st->same_pairs;
+        if (st->components > 1 && st->err_kind == 0) atomicAdd(&more[r], 1);
+    }
+}
+
+// f64 MST weight of fit blockIdx.x in forest_mst_weight's order: the partial of block b of its
+// grid is the tree sum over edges b * 256 + t + i * grid * 256, then the partials' tree sum.
+__global__ void __launch_bounds__(kWeightThreads)
+    pack_weight_kernel(const PackFit *__restrict__ fits) {
+    __shared__ double sh[kWeightThreads];
+    __shared__ double partials[kWeightBlocks];
+    const PackFit &f = fits[blockIdx.x];
+    DevStatus *st = f.status;
+    if (st->err_kind) return;
+    // a complete forest has n - 1 edges (any other count is reported by the host)
+    const int64_t m = (int64_t)st->edges < f.n - 1 ? (int64_t)st->edges : f.n - 1;
+    if (m <= 0) {
+        if (threadIdx.x == 0) st->mst_weight = 0.0;
+        return;
+    }
+    const int64_t g = ceil_div(m, kWeightThreads);
+    const int grid = (int)(g < kWeightBlocks ? g : kWeightBlocks);
+    for (int b = 0; b < grid; ++b) {
+        double acc = 0.0;
+        for (int64_t i = (int64_t)b * kWeightThreads + threadIdx.x; i < m;
+             i += (int64_t)grid * kWeightThreads)
+            acc += sqrt((double)f.w[i]);
+        const double total = block_tree_sum(acc, sh);
+        if (threadIdx.x == 0) partials[b] = total;
+        __syncthreads();
+    }
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < grid; i += kWeightThreads) acc += partials[i];
+    const double total = block_tree_sum(acc, sh);
+    if (threadIdx.x == 0) st->mst_weight = total;
+}
+
+}  // namespace
+
+int pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+             int k_max, int splits, cudaStream_t s, int64_t &launches) {
+    return launch_pack_knn(ctx, fits, count, n_max, d_max, k_max, splits, s, launches);
+}
+
+int pack_seed(cuscan_ctx *ctx, const PackFit *fits, int count, int *more, cudaStream_t s) {
+    CUSCAN_KERNEL(pack_seed_kernel, count, SCAN_THREADS, 0, s, fits, more);
+    CUSCAN_LAUNCH(ctx, "pack_seed_kernel");
+    return CUSCAN_OK;
+}
+
+int pack_round(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+               int splits, int r, int *more, cudaStream_t s) {
+    CUSCAN_KERNEL(pack_sort_kernel, count, SCAN_THREADS, 0, s, fits);
+    CUSCAN_LAUNCH(ctx, "pack_sort_kernel");
+    if (int rc = launch_pack_candidates(ctx, fits, count, n_max, d_max, splits, s)) return rc;
+    CUSCAN_KERNEL(pack_merge_kernel, count, SCAN_THREADS, 0, s, fits, r, more);
+    CUSCAN_LAUNCH(ctx, "pack_merge_kernel");
+    return CUSCAN_OK;
+}
+
+int pack_weight(cuscan_ctx *ctx, const PackFit *fits, int count, cudaStream_t s) {
+    CUSCAN_KERNEL(pack_weight_kernel, count, kWeightThreads, 0, s, fits);
+    CUSCAN_LAUNCH(ctx, "pack_weight_kernel");
+    return CUSCAN_OK;
 }
 
 }  // namespace cuscan

@@ -92,4 +92,51 @@ int forest_mst_weight(cuscan_ctx *ctx, ForestBuffers &b, const float *w, int64_t
 int scan_exclusive(cuscan_ctx *ctx, const int32_t *in, int32_t *out, int64_t n,
                    int32_t *grand_total, Buffer &tmp, cudaStream_t s);
 
+// ---- packed small fits (pack.cu): one launch per step for every fit of a pack ----
+// One fit of a pack: its sizes and every device buffer its steps use. An array of these sits
+// in device memory; the grouped kernels take fit blockIdx.z (kNN, candidates) or blockIdx.x
+// (the one-CTA forest steps) from it.
+struct PackFit {
+    const float *x;  // n x d rows
+    int64_t n;
+    int d, k, min_samples, allow_empty;
+    int32_t *ids;
+    float *dsq, *core;
+    int32_t *label;
+    uint32_t *src, *dst;
+    float *w;
+    int32_t *next, *ja, *ma, *jb, *mb, *keep, *pos, *parent, *minlab;
+    int32_t *kept_total;  // [0] kept edges of the last merge, [1] this round runs (0/1)
+    uint32_t *esrc, *edst;
+    float *ew;
+    int32_t *cnt, *start, *fill, *perm, *labp;
+    float *xp, *corep;
+    unsigned long long *row_keys, *comp_keys;
+    int32_t *tile_lo, *tile_hi;
+    int32_t *part_ids;  // kNN partial lists when the reference range is split
+    float *part_dist;
+    DevStatus *status;
+};
+constexpr int kPackMaxRounds = 64;  // the host driver's round limit (api.cu)
+constexpr int kPackErrNoConvergence = 8;
+// Exact kNN lists of every fit whose k is at most 32 (squared distances, self excluded), the
+// reference range of each fit split in `splits` chunks (partial lists merged when > 1).
+int pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+             int k_max, int splits, cudaStream_t s, int64_t &launches);
+// Core column, kNN seed and its merge (forest_core + forest_seed) of every fit; zeroes the
+// fits' status blocks and the pack's per-round counters more[0, kPackMaxRounds + 2).
+int pack_seed(cuscan_ctx *ctx, const PackFit *fits, int count, int *more, cudaStream_t s);
+// One Borůvka round r of every fit that still has more than one component: the component
+// sort, the exact candidate sweep, the winners and the merge. more[r] counts the fits that
+// need another round after it.
+int pack_round(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+               int splits, int r, int *more, cudaStream_t s);
+// status->mst_weight of every fit without an error (forest_mst_weight's order).
+int pack_weight(cuscan_ctx *ctx, const PackFit *fits, int count, cudaStream_t s);
+// Grouped launches inside other translation units (knn.cu, boruvka.cu).
+int launch_pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+                    int k_max, int splits, cudaStream_t s, int64_t &launches);
+int launch_pack_candidates(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max,
+                           int d_max, int splits, cudaStream_t s);
+
 }  // namespace cuscan

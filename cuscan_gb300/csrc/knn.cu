@@ -15,7 +15,7 @@
 // across blocks and the partial lists are merged by a second kernel.
 #include <limits>
 
-#include "common.cuh"
+#include "forest.cuh"
 
 namespace cuscan {
 namespace {
@@ -69,23 +69,19 @@ __device__ __forceinline__ void list_insert(float (&ld)[K], int (&li)[K], float 
     }
 }
 
-// One block: QB query rows x reference rows [r_begin, r_end). Writes the K-best list of each
-// query (first k entries) to out_ids/out_dist rows of width k (partial lists when split).
+// One block: QB query rows [q0, q0 + QB) x reference rows [r_begin, r_end). Writes the K-best
+// list of each query (first k entries) to out_ids/out_dist rows of width k, at split * stride
+// (partial lists when split); with stride 0 a query qi goes to row qmap[qi] when qmap is set.
 template <int K>
-__global__ void __launch_bounds__(QB) knn_fp32_kernel(
+__device__ __forceinline__ void knn_block(
     const float *__restrict__ query, int64_t nq, const float *__restrict__ ref, int64_t nr, int d,
-    int k, int exclude_self, int64_t query_offset, float pad, int64_t ref_chunk,
-    int32_t *__restrict__ out_ids, float *__restrict__ out_dist, int64_t out_split_stride,
-    const int32_t *__restrict__ qmap) {
-    extern __shared__ __align__(16) float smem[];
+    int k, int exclude_self, int64_t query_offset, float pad, int64_t q0, int64_t r_begin,
+    int64_t r_end, int32_t *__restrict__ out_ids, float *__restrict__ out_dist,
+    int64_t out_split_stride, int64_t split, const int32_t *__restrict__ qmap, float *smem) {
     float *qs = smem;                         // [d][QB]
     float *tiles = smem + (size_t)d * QB;     // 2 x [d][RTP]
     const int tid = threadIdx.x;
-    const int64_t q0 = (int64_t)blockIdx.x * QB;
     const int64_t qi = q0 + tid;
-    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
-    int64_t r_end = r_begin + ref_chunk;
-    if (r_end > nr) r_end = nr;
 
     // stage this block's queries transposed (qmap selects a subset of query rows)
     for (int e = tid; e < QB * d; e += QB) {
@@ -154,8 +150,8 @@ __global__ void __launch_bounds__(QB) knn_fp32_kernel(
     if (qi < nq) {
         // partial lists (split > 1) stay compact; final rows go to their mapped row
         const int64_t orow = (qmap && out_split_stride == 0) ? (int64_t)qmap[qi] : qi;
-        int32_t *oi = out_ids + (int64_t)blockIdx.y * out_split_stride + orow * k;
-        float *od = out_dist + (int64_t)blockIdx.y * out_split_stride + orow * k;
+        int32_t *oi = out_ids + split * out_split_stride + orow * k;
+        float *od = out_dist + split * out_split_stride + orow * k;
 #pragma unroll
         for (int s = 0; s < K; ++s) {
             if (s < k) {
@@ -166,16 +162,51 @@ __global__ void __launch_bounds__(QB) knn_fp32_kernel(
     }
 }
 
-// Merge `splits` sorted partial lists per query into the final top-k.
 template <int K>
-__global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
-                                 const float *__restrict__ part_dist, int64_t nq, int k,
-                                 int splits, int64_t split_stride, float pad, int64_t nr,
-                                 int squared, int32_t *__restrict__ ids, float *__restrict__ dist,
-                                 const int32_t *__restrict__ qmap) {
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
-    const int64_t orow = qmap ? (int64_t)qmap[q] : q;
+__global__ void __launch_bounds__(QB) knn_fp32_kernel(
+    const float *__restrict__ query, int64_t nq, const float *__restrict__ ref, int64_t nr, int d,
+    int k, int exclude_self, int64_t query_offset, float pad, int64_t ref_chunk,
+    int32_t *__restrict__ out_ids, float *__restrict__ out_dist, int64_t out_split_stride,
+    const int32_t *__restrict__ qmap) {
+    extern __shared__ __align__(16) float smem[];
+    const int64_t r_begin = (int64_t)blockIdx.y * ref_chunk;
+    int64_t r_end = r_begin + ref_chunk;
+    if (r_end > nr) r_end = nr;
+    knn_block<K>(query, nq, ref, nr, d, k, exclude_self, query_offset, pad,
+                 (int64_t)blockIdx.x * QB, r_begin, r_end, out_ids, out_dist, out_split_stride,
+                 (int64_t)blockIdx.y, qmap, smem);
+}
+
+// Packed fits: fit blockIdx.z, query block blockIdx.x, reference chunk blockIdx.y of `splits`
+// (the self-kNN of launch_exact_knn_fp32: squared distances, self excluded, +inf padding).
+// Fits with k > K take the per-fit launch instead.
+template <int K>
+__global__ void __launch_bounds__(QB) pack_knn_kernel(const PackFit *__restrict__ fits,
+                                                      int splits) {
+    extern __shared__ __align__(16) float smem[];
+    const PackFit &f = fits[blockIdx.z];
+    const int64_t n = f.n, q0 = (int64_t)blockIdx.x * QB;
+    const int k = f.k;
+    if (k > K || q0 >= n) return;
+    const int64_t chunk = ceil_div(ceil_div(n, (int64_t)splits), (int64_t)RT) * RT;
+    const int64_t r_begin = (int64_t)blockIdx.y * chunk;
+    const int64_t r_end = r_begin + chunk < n ? r_begin + chunk : n;
+    if (splits > 1)
+        knn_block<K>(f.x, n, f.x, n, f.d, k, 1, 0, CUSCAN_INF, q0, r_begin, r_end, f.part_ids,
+                     f.part_dist, n * k, (int64_t)blockIdx.y, nullptr, smem);
+    else
+        knn_block<K>(f.x, n, f.x, n, f.d, k, 1, 0, CUSCAN_INF, q0, r_begin, r_end, f.ids, f.dsq,
+                     0, 0, nullptr, smem);
+}
+
+// Merge `splits` sorted partial lists of query q into the final top-k (row orow).
+template <int K>
+__device__ __forceinline__ void knn_merge_row(const int32_t *__restrict__ part_ids,
+                                              const float *__restrict__ part_dist, int64_t q,
+                                              int64_t orow, int k, int splits,
+                                              int64_t split_stride, float pad, int64_t nr,
+                                              int squared, int32_t *__restrict__ ids,
+                                              float *__restrict__ dist) {
     float ld[K];
     int li[K];
 #pragma unroll
@@ -200,6 +231,28 @@ __global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
             dist[orow * k + s] = squared ? x : sqrtf(x);
         }
     }
+}
+
+template <int K>
+__global__ void knn_merge_kernel(const int32_t *__restrict__ part_ids,
+                                 const float *__restrict__ part_dist, int64_t nq, int k,
+                                 int splits, int64_t split_stride, float pad, int64_t nr,
+                                 int squared, int32_t *__restrict__ ids, float *__restrict__ dist,
+                                 const int32_t *__restrict__ qmap) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    knn_merge_row<K>(part_ids, part_dist, q, qmap ? (int64_t)qmap[q] : q, k, splits, split_stride,
+                     pad, nr, squared, ids, dist);
+}
+
+// Packed fits: the partial lists of fit blockIdx.y merged into its kNN lists.
+template <int K>
+__global__ void pack_knn_merge_kernel(const PackFit *__restrict__ fits, int splits) {
+    const PackFit &f = fits[blockIdx.y];
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f.k > K || q >= f.n) return;
+    knn_merge_row<K>(f.part_ids, f.part_dist, q, q, f.k, splits, f.n * f.k, CUSCAN_INF, f.n, 1,
+                     f.ids, f.dsq);
 }
 
 __global__ void sqrt_rows_kernel(float *dist, int64_t count) {
@@ -373,6 +426,32 @@ int launch_exact_knn_fp32(cuscan_ctx *ctx, const float *query, int64_t nq, const
         CUSCAN_LAUNCH(ctx, "sqrt_rows_kernel");
     }
     return CUSCAN_OK;
+}
+
+template <int K>
+static int run_pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max,
+                        int d_max, int splits, cudaStream_t s, int64_t &launches) {
+    const size_t smem = ((size_t)d_max * QB + 2 * (size_t)d_max * RTP) * sizeof(float);
+    if (int rc = allow_dynamic_smem(ctx, pack_knn_kernel<K>, smem)) return rc;
+    dim3 grid((unsigned)ceil_div(n_max, QB), (unsigned)splits, (unsigned)count);
+    CUSCAN_KERNEL(pack_knn_kernel<K>, grid, QB, smem, s, fits, splits);
+    ++launches;
+    if (splits > 1) {
+        dim3 mg((unsigned)ceil_div(n_max, 128), (unsigned)count);
+        CUSCAN_KERNEL(pack_knn_merge_kernel<K>, mg, 128, 0, s, fits, splits);
+        ++launches;
+    }
+    CUSCAN_LAUNCH(ctx, "pack_knn_kernel");
+    return CUSCAN_OK;
+}
+
+int launch_pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
+                    int k_max, int splits, cudaStream_t s, int64_t &launches) {
+    if (((size_t)d_max * QB + 2 * (size_t)d_max * RTP) * sizeof(float) > 200 * 1024)
+        return fail(ctx, CUSCAN_CAPACITY, "feature count %d exceeds the kNN staging limit", d_max);
+    if (k_max <= 8) return run_pack_knn<8>(ctx, fits, count, n_max, d_max, splits, s, launches);
+    if (k_max <= 16) return run_pack_knn<16>(ctx, fits, count, n_max, d_max, splits, s, launches);
+    return run_pack_knn<32>(ctx, fits, count, n_max, d_max, splits, s, launches);
 }
 
 }  // namespace cuscan

@@ -15,8 +15,8 @@
 //
 // Small fits are packed: a slot that admits a fit of at most CUSCAN_PACK_MAX_ROWS rows at the
 // head of the queue also takes the small fits queued right behind it (in order, up to the pack
-// limit, while the budget allows) and runs them in one CUDA graph launch
-// (cuscan_fit_core_packed). A pack commits the sum of its requests' bounds on top of the
+// limit, while the budget allows) and runs them as one pack (cuscan_fit_core_packed: each step
+// of every fit in one launch). A pack commits the sum of its requests' bounds on top of the
 // workspace the slot holds, since its fits use buffers of their own.
 //
 // A request runs the estimator flow of crates/hdbscan/src/estimator.rs:1034-1392 for one
@@ -95,7 +95,7 @@ struct Slot {
     int64_t running = 0;    // admission bound of the request it runs (sum over a pack)
     Task task = Task::None;
     Request *req = nullptr;
-    std::vector<Request *> pack;  // two or more small fits run in one graph launch
+    std::vector<Request *> pack;  // two or more small fits run as one pack
     std::condition_variable cv;
 };
 
@@ -262,7 +262,7 @@ void DeviceExecutor::run(Slot &slot, Request &r) {
     finish(r, f, o);
 }
 
-// Small fits of one pack: finite split of each, one graph launch for all fit cores, then the
+// Small fits of one pack: finite split of each, one packed call for all fit cores, then the
 // extraction of each.
 void DeviceExecutor::run_pack(Slot &slot, std::vector<Request *> &pack) {
     const size_t count = pack.size();
@@ -332,10 +332,10 @@ struct cuscan_server {
     int64_t next_id = 1;
     int64_t submitted = 0, completed = 0, failed = 0, releases = 0;
     int64_t peak_committed = 0;
-    // Off by default: with several slots, building a graph per pack costs more host time
-    // (capture and instantiation, serialised across slot threads) than the slots' ordinary
-    // launches of the same fits overlap away.
-    int32_t pack_limit = 1;
+    // Packs of up to 8 small fits by default: a pack launches each step once for all of its
+    // fits and reads the host once per few rounds, where eight slots running one small fit
+    // each launch every step eight times and read the host once per round each.
+    int32_t pack_limit = 8;
     int64_t packs = 0, packed_requests = 0;
     Clock::time_point t0 = Clock::now();
     bool stopping = false;
@@ -384,7 +384,7 @@ struct cuscan_server {
                 best->running = r->bytes;
                 r->slot = index_of(best);
                 r->t_admit = Clock::now();
-                // small fits queued right behind a small head join it in one graph launch
+                // small fits queued right behind a small head join it in one pack
                 if (small_fit(r) && pack_limit > 1) {
                     int64_t sum = r->bytes;
                     std::vector<Request *> pack{r};

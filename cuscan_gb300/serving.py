@@ -61,14 +61,14 @@ class FitServer:
     free memory (16 GiB for the simulated server).
 
     ``pack_limit`` is the most small fits (at most ``_lib.PACK_MAX_ROWS`` rows) a slot runs
-    together in one CUDA graph launch; 1 (the default) runs every fit on its own, which is
-    faster when several slots share the host (see ``cuscan_server_set_pack_limit``).
+    together as one pack, each step of every fit in one launch; 8 by default, 1 runs every fit
+    on its own (see ``cuscan_server_set_pack_limit``).
 
     ``simulated_us_per_kpoint`` builds the scheduling test double instead: the same queue and
     admission with slots that run no fit (no GPU needed; results cannot be read)."""
 
     def __init__(self, device: int = 0, slots: int = 4, budget_bytes: int | None = None, *,
-                 pack_limit: int = 1, simulated_us_per_kpoint: float | None = None):
+                 pack_limit: int = 8, simulated_us_per_kpoint: float | None = None):
         if budget_bytes is None:
             budget_bytes = (16 << 30 if simulated_us_per_kpoint is not None
                             else default_budget(device))

@@ -209,15 +209,16 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
  * Packed small fits (no reference counterpart; each fit is the core_distances + spanning_tree
  * body of crates/hdbscan/src/estimator.rs:524-874, as in cuscan_fit_core). Up to
  * CUSCAN_PACK_MAX_FITS independent point sets of at most CUSCAN_PACK_MAX_ROWS rows each are fit
- * in ONE CUDA graph launch: the graph holds one branch per fit (copy in, exact kNN, core
- * distances, kNN seed, the Borůvka rounds as a device-controlled while loop, f64 MST weight,
- * copy out), so the fits overlap on the device and no host round trip happens between rounds.
- * At these sizes every precision runs the exact f32 kernels, so each item's outputs are bit
- * identical to cuscan_fit_core's for the same input. The graph is captured and instantiated on
- * every call. Host pointers; the call synchronises the context stream before returning.
+ * together, each step of every fit in one launch: one copy in (every fit's rows), the exact kNN
+ * lists, the core column with the kNN seed, the Borůvka rounds (component sort, candidate
+ * sweep, merge: three launches per round for the whole pack; a fit whose forest is complete
+ * skips the rest on the device), the f64 MST weight, one copy out. The host reads one counter
+ * after the first three rounds and after every two more. At these sizes every precision runs
+ * the exact f32 kernels, so each item's outputs are bit identical to cuscan_fit_core's for the
+ * same input. Host pointers; the call synchronises the context stream before returning.
  * Each item's status is set; the call returns the first failing item's status (message in
- * cuscan_last_error), or CUSCAN_OK. Stats: core_ms covers the copy in, the kNN sweep and the
- * core column of the item's branch, mst_ms the seed, the rounds, the weight and the copy out;
+ * cuscan_last_error), or CUSCAN_OK. Stats are the pack's: core_ms and knn_kernel_ms cover the
+ * copy in and the kNN lists, mst_ms the core column, seed, rounds and weight;
  * candidate_kernel_ms is 0 (the rounds are not timed one by one).
  */
 #define CUSCAN_PACK_MAX_FITS 16
@@ -241,12 +242,11 @@ typedef struct cuscan_fit_item {
 } cuscan_fit_item;
 int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, int32_t count);
 /*
- * How the context's packed fits reached their graphs so far (no reference counterpart): packs
- * whose graph was instantiated, and packs that updated the graph instantiated for an earlier
- * pack of the same size in place. Either pointer may be NULL.
+ * The context's latest pack (no reference counterpart): the kernels it launched and the host
+ * reads of its round counter between the copy in and the copy out. Either pointer may be NULL.
  */
-int cuscan_fit_core_packed_graph_stats(cuscan_ctx *ctx, int64_t *instantiations,
-                                       int64_t *updates);
+int cuscan_fit_core_packed_launch_stats(cuscan_ctx *ctx, int64_t *launches,
+                                        int64_t *host_reads);
 
 /*
  * Per Borůvka round of the context's last fit (no reference counterpart; the reference logs
@@ -472,7 +472,7 @@ typedef struct cuscan_server_info {
     int32_t status;          /* outcome once finished; CUSCAN_PENDING while queued or running */
     int32_t slot;            /* slot that ran it, -1 before admission */
     int32_t kind;            /* 0 fit, 1 approximate_predict */
-    int32_t pack_size;       /* fits in the graph launch that ran it (1: run on its own) */
+    int32_t pack_size;       /* fits in the pack that ran it (1: run on its own) */
     int64_t n;
     int64_t finite_rows;
     int32_t d;
@@ -497,7 +497,7 @@ typedef struct cuscan_server_stats {
     int64_t committed_bytes;       /* current sum of slot commitments */
     int64_t peak_committed_bytes;  /* largest sum at any admission */
     int64_t workspace_releases;    /* idle-slot releases ordered by admission */
-    int64_t packs;                 /* graph launches that ran two or more small fits */
+    int64_t packs;                 /* packs that ran two or more small fits */
     int64_t packed_requests;       /* fit requests those launches ran */
 } cuscan_server_stats;
 
@@ -538,14 +538,13 @@ int cuscan_server_request_error(cuscan_server *server, int64_t request_id, char 
 /* Drop a finished request's results. */
 int cuscan_server_release(cuscan_server *server, int64_t request_id);
 int cuscan_server_get_stats(cuscan_server *server, cuscan_server_stats *out);
-/* Most small fits (at most CUSCAN_PACK_MAX_ROWS rows) one slot runs together in one graph
- * launch (cuscan_fit_core_packed), 1 .. CUSCAN_PACK_MAX_FITS; 1 turns packing off. When a
- * slot admits a small fit at the head of the queue it also takes the small fits queued right
- * behind it, in order, while the pack limit and the memory budget allow (a pack commits the
- * sum of its requests' bounds on top of the workspace the slot holds). Default 1: with
- * several slots the host time of building one graph per pack (capture and instantiation,
- * serialised across slot threads) outweighs what it saves; packing pays when one host thread
- * issues many small fits. */
+/* Most small fits (at most CUSCAN_PACK_MAX_ROWS rows) one slot runs together as one pack
+ * (cuscan_fit_core_packed), 1 .. CUSCAN_PACK_MAX_FITS; 1 turns packing off. When a slot admits
+ * a small fit at the head of the queue it also takes the small fits queued right behind it, in
+ * order, while the pack limit and the memory budget allow (a pack commits the sum of its
+ * requests' bounds on top of the workspace the slot holds). Default 8: a pack launches each
+ * step once for all of its fits, so eight slots running packs launch and synchronise far less
+ * than eight slots running one small fit each. */
 int cuscan_server_set_pack_limit(cuscan_server *server, int32_t max_fits);
 
 #ifdef __cplusplus

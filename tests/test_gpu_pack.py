@@ -1,5 +1,5 @@
-"""Packed small fits (cuscan_fit_core_packed): several fit cores in one CUDA graph launch, the
-Borůvka rounds of each as a device-controlled while loop.
+"""Packed small fits (cuscan_fit_core_packed): several fit cores together, each step of every
+fit in one launch, the Borůvka rounds of finished fits skipped on the device.
 
 Every fit of a pack must equal the same fit run alone through cuscan_fit_core, and the oracle,
 bit for bit: kNN ids and distances, core distances, MST edges in merge order, round and seed
@@ -64,26 +64,49 @@ def test_consecutive_packs_reuse_the_workspace(gpu_ctx):
             assert_fit_equal(got, O.fit_core(x, ms))
 
 
-def test_packs_of_one_size_update_one_instantiated_graph():
-    """Packs of the same size share one graph topology: the first is instantiated, the later
-    ones (other row counts, dimensions and point sets) update it in place, and every result
-    still equals the oracle. Row counts stay above 256, where the exact kNN always splits the
-    reference range (at most 256 rows take the unsplit launch, another topology, and such a pack
-    is instantiated anew)."""
+def test_pack_launches_each_step_once_for_all_fits():
+    """A pack launches each step once for all of its fits: the kNN lists (and their merge), the
+    seed, three launches per round and the weight, with one host read of the round counter
+    after the first three rounds and after every two more. The counts do not grow with the
+    number of fits, and every result still equals the oracle."""
     ctx = _lib.Context(0)
     rng = np.random.default_rng(9)
-    rounds = 4
-    for r in range(rounds):
+    for count in (1, 5, 16):
         fits = [(synthetic.blobs_with_noise(n=int(rng.integers(300, 2048)),
                                             d=int(rng.choice([8, 32, 64])),
                                             centers=int(rng.integers(2, 20)),
                                             seed=int(rng.integers(1 << 30))), 5,
-                 _lib.PRECISION_FP16_REFINED) for _ in range(3)]
+                 _lib.PRECISION_FP16_REFINED) for _ in range(count)]
         packed = ctx.fit_core_packed(fits)
+        rounds = max(got["stats"]["rounds"] for got in packed)
         for (x, ms, _), got in zip(fits, packed):
             assert_fit_equal(got, O.fit_core(x, ms))
-    st = ctx.packed_graph_stats()
-    assert st == {"instantiations": 1, "updates": rounds - 1}, st
+        st = ctx.packed_launch_stats()
+        launched = 3 if rounds <= 3 else 3 + 2 * ((rounds - 2) // 2)
+        assert st["host_reads"] == 1 + (launched - 3) // 2, (st, rounds)
+        # kNN (+ merge), seed, three per round launched, weight
+        assert st["launches"] in (3 + 3 * launched, 4 + 3 * launched), (st, rounds)
+
+
+def test_pack_with_wide_lists_and_tiny_fits(gpu_ctx):
+    """k > 32 takes the per-fit kNN launch inside the pack; fits of 2 and 3 rows, and a fit
+    whose min_samples exceeds its rows, sit beside ordinary ones."""
+    rng = np.random.default_rng(21)
+    fits = [(rng.normal(size=(400, 6)).astype(np.float32), 40, _lib.PRECISION_PLAIN),
+            (rng.normal(size=(2, 3)).astype(np.float32), 5, _lib.PRECISION_PLAIN),
+            (rng.normal(size=(3, 3)).astype(np.float32), 2, _lib.PRECISION_BF16_REFINED),
+            (rng.normal(size=(30, 2)).astype(np.float32), 50, _lib.PRECISION_PLAIN),
+            (synthetic.blobs_with_noise(n=1200, d=40, centers=7, seed=8), 5,
+             _lib.PRECISION_FP16_REFINED)]
+    packed = gpu_ctx.fit_core_packed(fits)
+    for (x, ms, prec), got in zip(fits, packed):
+        alone = gpu_ctx.fit_core(x, ms, prec)
+        for key in ("knn_ids", "src", "dst"):
+            np.testing.assert_array_equal(got[key], alone[key])
+        for key in ("knn_sq", "core_sq", "wsq"):
+            np.testing.assert_array_equal(bits(got[key]), bits(alone[key]))
+        assert got["stats"]["mst_weight"] == alone["stats"]["mst_weight"]
+        assert_fit_equal(got, O.fit_core(x, ms))
 
 
 def test_pack_limits(gpu_ctx):
