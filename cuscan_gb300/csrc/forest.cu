@@ -952,9 +952,9 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 }
 
 // Start of round r of fit blockIdx.x: whether it runs (more than one component, no error,
-// within the round limit: the host driver's checks), then the component sort, the sorted copies
-// (gather_kernel), cleared row keys and the label range of every 32-row tile
-// (tile_range_kernel).
+// within the round limit: the host driver's checks), then the component sort, the sorted labels
+// and core distances (gather_kernel; pack_gather_kernel copies the rows), cleared row keys and
+// the label range of every 32-row tile (tile_range_kernel).
 __global__ void __launch_bounds__(SCAN_THREADS) pack_sort_kernel(const PackFit *__restrict__ fits) {
     const PackFit &f = fits[blockIdx.x];
     const int tid = threadIdx.x;
@@ -974,18 +974,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) pack_sort_kernel(const PackFit *
     if (!run) return;
     sort_block(f.label, n, f.cnt, f.start, f.fill, f.perm, st);
     __syncthreads();
-    const int d = f.d;
-    for (int64_t e = tid; e < n * d; e += SCAN_THREADS) {
-        const int64_t p = e / d;
-        const int c = (int)(e - p * d);
+    for (int64_t p = tid; p < n; p += SCAN_THREADS) {
         const int32_t i = f.perm[p];
-        f.xp[e] = f.x[(int64_t)i * d + c];
-        if (c == 0) {
-            f.corep[p] = f.core[i];
-            f.labp[p] = f.label[i];
-        }
+        f.corep[p] = f.core[i];
+        f.labp[p] = f.label[i];
+        f.row_keys[p] = ~0ull;
     }
-    for (int64_t i = tid; i < n; i += SCAN_THREADS) f.row_keys[i] = ~0ull;
     __syncthreads();
     const int64_t tiles = ceil_div(n, kPackRowTile);
     for (int64_t t = tid; t < tiles; t += SCAN_THREADS) {
@@ -998,6 +992,22 @@ __global__ void __launch_bounds__(SCAN_THREADS) pack_sort_kernel(const PackFit *
         }
         f.tile_lo[t] = mn;
         f.tile_hi[t] = mx;
+    }
+}
+
+// Sorted copy of the rows of fit blockIdx.y whose round runs (gather_kernel's copy), spread over
+// the grid's x blocks: a single CTA per fit would wait on one dependent load pair per element.
+__global__ void pack_gather_kernel(const PackFit *__restrict__ fits) {
+    const PackFit &f = fits[blockIdx.y];
+    if (!*(volatile int32_t *)&f.kept_total[1]) return;
+    const int64_t n = f.n;
+    const int d = f.d;
+    const int64_t total = n * d;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = e / d;
+        const int c = (int)(e - p * d);
+        f.xp[e] = f.x[(int64_t)f.perm[p] * d + c];
     }
 }
 
@@ -1072,6 +1082,9 @@ int pack_round(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, i
                int splits, int r, int *more, cudaStream_t s) {
     CUSCAN_KERNEL(pack_sort_kernel, count, SCAN_THREADS, 0, s, fits);
     CUSCAN_LAUNCH(ctx, "pack_sort_kernel");
+    const dim3 gg((unsigned)std::min<int64_t>(ceil_div(n_max * d_max, 256), 128), (unsigned)count);
+    CUSCAN_KERNEL(pack_gather_kernel, gg, 256, 0, s, fits);
+    CUSCAN_LAUNCH(ctx, "pack_gather_kernel");
     if (int rc = launch_pack_candidates(ctx, fits, count, n_max, d_max, splits, s)) return rc;
     CUSCAN_KERNEL(pack_merge_kernel, count, SCAN_THREADS, 0, s, fits, r, more);
     CUSCAN_LAUNCH(ctx, "pack_merge_kernel");

@@ -13,8 +13,8 @@ struct DevStatus {
     int err_kind;          // 0 ok, 1 numerical weight, 2 index out of range, 4 no progress
     int pad[3];
     double mst_weight;     // f64 total MST weight, written once after the last round
-    // kept on the device by fits whose round loop runs inside a CUDA graph (no host read
-    // between rounds): the seed's results, rounds run and ordered cross pairs entering them
+    // kept on the device by packed fits (no host read after every round): the seed's results,
+    // rounds run and ordered cross pairs entering them
     unsigned long long seed_edges;
     unsigned long long components_after_seed;
     unsigned long long rounds;
@@ -127,8 +127,8 @@ int pack_knn(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int
 // fits' status blocks and the pack's per-round counters more[0, kPackMaxRounds + 2).
 int pack_seed(cuscan_ctx *ctx, const PackFit *fits, int count, int *more, cudaStream_t s);
 // One Borůvka round r of every fit that still has more than one component: the component
-// sort, the exact candidate sweep, the winners and the merge. more[r] counts the fits that
-// need another round after it.
+// sort, the sorted copy of the rows, the exact candidate sweep, the winners and the merge.
+// more[r] counts the fits that need another round after it.
 int pack_round(cuscan_ctx *ctx, const PackFit *fits, int count, int64_t n_max, int d_max,
                int splits, int r, int *more, cudaStream_t s);
 // status->mst_weight of every fit without an error (forest_mst_weight's order).

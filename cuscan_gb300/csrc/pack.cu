@@ -13,13 +13,14 @@
 //      each fit is split to fill the GPU);
 //   3. core column, kNN seed and its merge, one CTA per fit (pack_seed_kernel);
 //   4. Borůvka rounds: per round the component sort (pack_sort_kernel, one CTA per fit), the
-//      exact candidate sweep (pack_candidates_kernel) and the winners and merge
-//      (pack_merge_kernel, one CTA per fit). A fit whose forest is complete skips the rest of
-//      the rounds on the device. The host launches rounds in batches (three, then two at a
-//      time) and reads one counter after each batch: the fits that need another round;
+//      sorted copy of the rows (pack_gather_kernel), the exact candidate sweep
+//      (pack_candidates_kernel) and the winners and merge (pack_merge_kernel, one CTA per
+//      fit). A fit whose forest is complete skips the rest of the rounds on the device. The
+//      host launches rounds in batches (three, then two at a time) and reads one counter after
+//      each batch: the fits that need another round;
 //   5. the f64 MST weight, one CTA per fit;
 //   6. one copy out: every fit's status block and outputs.
-// A pack of eight fits that finish in three rounds takes 12 launches and one host read between
+// A pack of eight fits that finish in three rounds takes 16 launches and one host read between
 // the copies, where the same fits alone take about 26 launches and 4 host reads each.
 //
 // Each step is the kernel body a fit alone runs for fewer than 2048 rows, in every precision
@@ -353,7 +354,7 @@ extern "C" int cuscan_fit_core_packed(cuscan_ctx *ctx, cuscan_fit_item *items, i
         for (int b = 0; b < batch && r < kPackMaxRounds + 2; ++b, ++r) {
             if ((rc = pack_round(ctx, fits, count, n_max, d_max, (int)splits, r, more, s)))
                 return rc;
-            P.launches += 3;
+            P.launches += 4;
         }
         int *due = reinterpret_cast<int *>(stg + L.more) + (r - 1);
         CUSCAN_CUDA(ctx, cudaMemcpyAsync(due, more + (r - 1), sizeof(int),

@@ -210,9 +210,9 @@ int cuscan_fit_core_device(cuscan_ctx *ctx, const float *data, int64_t n, int32_
  * body of crates/hdbscan/src/estimator.rs:524-874, as in cuscan_fit_core). Up to
  * CUSCAN_PACK_MAX_FITS independent point sets of at most CUSCAN_PACK_MAX_ROWS rows each are fit
  * together, each step of every fit in one launch: one copy in (every fit's rows), the exact kNN
- * lists, the core column with the kNN seed, the Borůvka rounds (component sort, candidate
- * sweep, merge: three launches per round for the whole pack; a fit whose forest is complete
- * skips the rest on the device), the f64 MST weight, one copy out. The host reads one counter
+ * lists, the core column with the kNN seed, the Borůvka rounds (component sort, sorted copy,
+ * candidate sweep, merge: four launches per round for the whole pack; a fit whose forest is
+ * complete skips the rest on the device), the f64 MST weight, one copy out. The host reads one counter
  * after the first three rounds and after every two more. At these sizes every precision runs
  * the exact f32 kernels, so each item's outputs are bit identical to cuscan_fit_core's for the
  * same input. Host pointers; the call synchronises the context stream before returning.

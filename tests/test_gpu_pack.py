@@ -66,7 +66,7 @@ def test_consecutive_packs_reuse_the_workspace(gpu_ctx):
 
 def test_pack_launches_each_step_once_for_all_fits():
     """A pack launches each step once for all of its fits: the kNN lists (and their merge), the
-    seed, three launches per round and the weight, with one host read of the round counter
+    seed, four launches per round and the weight, with one host read of the round counter
     after the first three rounds and after every two more. The counts do not grow with the
     number of fits, and every result still equals the oracle."""
     ctx = _lib.Context(0)
@@ -84,8 +84,8 @@ def test_pack_launches_each_step_once_for_all_fits():
         st = ctx.packed_launch_stats()
         launched = 3 if rounds <= 3 else 3 + 2 * ((rounds - 2) // 2)
         assert st["host_reads"] == 1 + (launched - 3) // 2, (st, rounds)
-        # kNN (+ merge), seed, three per round launched, weight
-        assert st["launches"] in (3 + 3 * launched, 4 + 3 * launched), (st, rounds)
+        # kNN (+ merge), seed, four per round launched, weight
+        assert st["launches"] in (3 + 4 * launched, 4 + 4 * launched), (st, rounds)
 
 
 def test_pack_with_wide_lists_and_tiny_fits(gpu_ctx):
