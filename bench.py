@@ -393,9 +393,10 @@ def serving_run(args, precision: str) -> dict:
 
 def small_fit_packing_section(args) -> dict:
     """The small requests of the fit stream (n <= 2047 rows, every d of the stream), all queued
-    at once, run with packing off (pack_limit 1: every fit on its own, about a hundred launches
-    and a host read per round) and on (up to 8 fits per pack, each step one launch for all). Throughput and
-    latency at saturation for both; the results are the same bits either way (GPU tests)."""
+    at once, run with packing off (pack_limit 1: every fit on its own, about 26 launches and a
+    host read per round each) and on (pack_limit 8, the default: each step one launch for all
+    fits of a pack). Throughput and latency at saturation for both; the results are the same
+    bits either way (GPU tests)."""
     import torch
 
     from cuscan_gb300 import _lib, synthetic
