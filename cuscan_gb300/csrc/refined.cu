@@ -71,6 +71,10 @@ struct Params {
     const int32_t *tile_hi;
     int64_t n, n_tiles, n_qblocks, n_chunks;
     int kblocks, stages;
+    // one-sided Borůvka with fewer query blocks than SMs: CTAs per query block, each running one
+    // contiguous part of the block's tile order (work item qi = block qi / splits, part qi %
+    // splits; appends then take their slots with atomics and the row bounds are min-reduced)
+    int splits;
     float c_a, one_minus_cb;
     int32_t *cand_ids;        // [n][M]
     float *cand_lb;           // [n][M]
@@ -591,8 +595,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     rot_val[rs] = rot;
                     mbar_arrive(&rot_full[rs]);
                 }
-                if (qi >= P.n_qblocks) break;
-                const int64_t qb = block_at<SYM>(P, qi);
+                if (qi >= P.n_qblocks * P.splits) break;
+                const int64_t qb = block_at<SYM>(P, qi / P.splits);
+                const int64_t part = qi % P.splits;
                 if (!mbar_wait(a_empty, a_phase ^ 1, abort, P.error)) break;
                 a_issued = 2u | a_phase;
                 a_phase ^= 1;
@@ -605,7 +610,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
-                for (int64_t i = 0; i < nvis; ++i) {
+                const int64_t i_hi = (part + 1) * nvis / P.splits;
+                for (int64_t i = part * nvis / P.splits; i < i_hi; ++i) {
                     const int64_t t = ROT ? (int64_t)knn_tile((int32_t)P.n_tiles, (int32_t)wa, rot, (int32_t)i)
                                           : vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
@@ -651,8 +657,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     qi = *(volatile int64_t *)&rot_blk[rs];
                     mbar_arrive(&rot_empty[rs]);
                 }
-                if (qi >= P.n_qblocks) break;
-                const int64_t qb = block_at<SYM>(P, qi);
+                if (qi >= P.n_qblocks * P.splits) break;
+                const int64_t qb = block_at<SYM>(P, qi / P.splits);
+                const int64_t part = qi % P.splits;
                 if (!mbar_wait(a_full, a_phase, abort, P.error)) break;
                 a_phase ^= 1;
                 fence_after();
@@ -660,8 +667,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 if (BORUVKA) qblock_range(P, qb, qlo, qhi);
                 const int64_t wa = window_start(P, qb);
                 const int64_t nvis = vis_count<SYM>(P, qb);
+                const int64_t i_hi = (part + 1) * nvis / P.splits;
                 bool ok = true;
-                for (int64_t i = 0; i < nvis; ++i) {
+                for (int64_t i = part * nvis / P.splits; i < i_hi; ++i) {
                     const int64_t t = vis_tile<SYM>(P, qb, wa, i);
                     if (tile_skipped<BORUVKA>(P, t, qlo, qhi)) continue;
                     const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
@@ -734,8 +742,9 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&rot_empty[rs]);
             }
-            if (qi >= P.n_qblocks) break;
-            const int64_t qb = block_at<SYM>(P, qi);
+            if (qi >= P.n_qblocks * P.splits) break;
+            const int64_t qb = block_at<SYM>(P, qi / P.splits);
+            const int64_t part = qi % P.splits;
             // the debug entry point dumps query block 0 against tile 0 (its first tile)
             const bool debug = P.debug_tile != nullptr && qb == 0;
             const int64_t row = qb * BM + row_local;  // query row
@@ -774,6 +783,8 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             if (BORUVKA) qblock_range(P, qb, qlo, qhi);
             const int64_t wa = window_start(P, qb);
             const int64_t nvis = vis_count<SYM>(P, qb);
+            // this work item's part [i_lo, i_hi) of the block's tile order
+            const int64_t i_lo = part * nvis / P.splits, i_hi = (part + 1) * nvis / P.splits;
             // symmetric mode: the warp's 32 rows summarised for the column-side block test
             float psmin_w = CUSCAN_INF, cmmax_w = 0.0f, coremin_w = CUSCAN_INF;
             if (SYM) {
@@ -788,7 +799,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             // next visited position i (>= i0) in this block's tile order, and its tile t_at
             int64_t t_at = 0;
             auto next_index = [&](int64_t i) -> int64_t {
-                for (; i < nvis; ++i) {
+                for (; i < i_hi; ++i) {
                     t_at = tile_at(i);
                     if (!tile_skipped<BORUVKA>(P, t_at, qlo, qhi)) break;
                 }
@@ -830,10 +841,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                     }
                 }
             };
-            int64_t ti = next_index(0);
-            if (ti < nvis) prefetch(t_at, tcount & 1);
+            int64_t ti = next_index(i_lo);
+            if (ti < i_hi) prefetch(t_at, tcount & 1);
             bool ok = true;
-            while (ti < nvis) {
+            while (ti < i_hi) {
                 const int64_t t = t_at;
                 const int64_t ti_next = next_index(ti + 1);
                 const uint32_t b = tcount & 1, tp = (tcount >> 1) & 1;
@@ -865,7 +876,7 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                 const int32_t ch_word = pre_ch;
                 const float comp_bound = pre_cb * P.s2;
                 __syncwarp();
-                if (ti_next < nvis) prefetch(t_at, b ^ 1);
+                if (ti_next < i_hi) prefetch(t_at, b ^ 1);
                 if (!mbar_wait(&t_full[b], tp, abort, P.error)) { ok = false; break; }
                 fence_after();
                 const uint32_t taddr =
@@ -1077,7 +1088,10 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
                                 const float lbw = fmaxf(fmaxf(lb, core_i), cj);
                                 const float Tn = fminf(U, comp_bound);
                                 if (lbw <= Tn) {
-                                    if (cnt < P.cap) P.cand_ids[(row * 2 + half) * P.cap + cnt] = (int32_t)j;
+                                    // split work items share the row's slots
+                                    const int slot = P.splits > 1
+                                        ? atomicAdd(&P.rowcnt[row * 2 + half], 1) : cnt;
+                                    if (slot < P.cap) P.cand_ids[(row * 2 + half) * P.cap + slot] = (int32_t)j;
                                     ++cnt;
                                     // upper bound of this pair's weight: D + eps = L + 2 eps
                                     const float eps2 =
@@ -1140,9 +1154,18 @@ __global__ void __launch_bounds__(THREADS, 1) screen_kernel(const Params P) {
             if (!ok) break;
             if (APPEND) {
                 // each half of a row appends into its own slot range [(2 row + half) * cap, +cap)
-                if (valid) P.rowcnt[row * 2 + half] = tau_ok ? cnt : P.cap + 1;
-                if (MODE == MODE_BORUVKA && valid && P.rowlb)
-                    P.rowlb[row * 2 + half] = __fmul_rd(lb_all, P.inv_s2);
+                if (valid && P.splits == 1) P.rowcnt[row * 2 + half] = tau_ok ? cnt : P.cap + 1;
+                if (MODE == MODE_BORUVKA && valid && P.rowlb) {
+                    const float lbr = __fmul_rd(lb_all, P.inv_s2);
+                    if (P.splits == 1) {
+                        P.rowlb[row * 2 + half] = lbr;
+                    } else {
+                        // the least over the block's parts; pair weights are >= 0, so a bound
+                        // below 0 is worth 0 and the bounds compare as unsigned bit patterns
+                        atomicMin(reinterpret_cast<unsigned int *>(P.rowlb) + row * 2 + half,
+                                  __float_as_uint(lbr > 0.0f ? lbr : 0.0f));
+                    }
+                }
             } else if (valid) {
                 const int64_t base_at = row * (2 * M) + half * M;
 #pragma unroll
@@ -1795,6 +1818,11 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.split = L.split;
     P.stages = L.stages;
     P.cursor = as<unsigned long long>(R.cursor);
+    P.splits = 1;
+    if (MODE == MODE_BORUVKA && P.n_qblocks > 0 && P.n_qblocks < ctx->sm_count && !debug_tile) {
+        const int64_t per = ctx->sm_count / P.n_qblocks;
+        P.splits = (int)(per < 16 ? per : 16);
+    }
     float ca, cb, abs_c;
     error_coefficients(d, L.d_pad, operand_format(R), R.fp16 ? R.amax_value * R.scale : R.amax_value, ca, cb, abs_c);
     P.c_a = ca;
@@ -1826,6 +1854,10 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
         P.capc = BORUVKA_COL_CAP;
     }
     if (MODE == MODE_BORUVKA) P.rowlb = Q.rowlb;
+    if (MODE == MODE_BORUVKA && P.splits > 1 && P.rowlb && P.nq > 0)
+        if (int rc = launch_fill_u64(ctx, reinterpret_cast<unsigned long long *>(P.rowlb), P.nq,
+                                     0x7f8000007f800000ull, s))  // +inf in both halves
+            return rc;
     if (MODE == MODE_KNN_THRESHOLD) {
         P.cap = KNN_CAP;
         P.cand_ids = Q.cand_ids;
@@ -1848,7 +1880,8 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     CUSCAN_LAUNCH(ctx, "screen_columns_kernel");
     auto kernel = screen_kernel<M, MODE>;
     if (int rc = allow_dynamic_smem(ctx, kernel, L.smem)) return rc;
-    int64_t grid = P.n_qblocks < ctx->sm_count ? P.n_qblocks : ctx->sm_count;
+    const int64_t items = P.n_qblocks * P.splits;
+    int64_t grid = items < ctx->sm_count ? items : ctx->sm_count;
     CUSCAN_KERNEL(kernel, (unsigned)grid, THREADS, L.smem, s, P);
     CUSCAN_LAUNCH(ctx, "screen_kernel");
     return CUSCAN_OK;
