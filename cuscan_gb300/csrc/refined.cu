@@ -1818,10 +1818,14 @@ static int run_screen(cuscan_ctx *ctx, RefinedBuffers &R, const Layout &L, int64
     P.split = L.split;
     P.stages = L.stages;
     P.cursor = as<unsigned long long>(R.cursor);
+    // parts of at least 128 tiles: the start of a work item (A tile, pipeline fill) stays small
+    // against its tiles, and the fits of a serving stream (under 32,768 rows) keep one CTA per
+    // block, leaving the other SMs to the fits running beside them
     P.splits = 1;
     if (MODE == MODE_BORUVKA && P.n_qblocks > 0 && P.n_qblocks < ctx->sm_count && !debug_tile) {
-        const int64_t per = ctx->sm_count / P.n_qblocks;
-        P.splits = (int)(per < 16 ? per : 16);
+        int64_t per = ctx->sm_count / P.n_qblocks;
+        if (per > P.n_tiles / 128) per = P.n_tiles / 128;
+        P.splits = (int)(per < 1 ? 1 : per < 16 ? per : 16);
     }
     float ca, cb, abs_c;
     error_coefficients(d, L.d_pad, operand_format(R), R.fp16 ? R.amax_value * R.scale : R.amax_value, ca, cb, abs_c);
